@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""Genotypes/s per power iteration (one pass Z = X^T X Omega) on GB300.
+
+Workload (default): the in-core mixed-precision configuration -- 50,000
+individuals x 1,000,000 SNPs (12.5 GB packed, HBM-resident), seeded
+Balding-Nichols cohort (K=8 populations, Dirichlet(1) sizes, Fst 0.02,
+p ~ U(0.01, 0.5), 2% missing), nrhs 40.  A step is one pass over the whole
+matrix; the packed matrix (12.5 GB) is far larger than L2, so no flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl dpca|reference]
+
+N > 1 runs N independent replicas (one per GPU; the path has no data-path
+collective) and reports the whole-job throughput.  Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "genotypes/s per power iter, mixed vs FP64 GPU @PC err≤1e-6; serve p50/p99"
+UNIT = "genotypes/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["dpca", "reference"], default="dpca")
+    p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    p.add_argument("--n-ind", type=int, default=50_000)
+    p.add_argument("--n-snp", type=int, default=1_000_000)
+    p.add_argument("--nrhs", type=int, default=40)
+    p.add_argument("--power", type=int, default=6)
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--cpu-snps", type=int, default=20_000, help="SNP rows in the CPU baseline sample")
+    p.add_argument("--fp64-snps", type=int, default=50_000, help="SNP rows for the plain FP64 GPU comparison")
+    p.add_argument("--accuracy-snps", type=int, default=100_000, help="SNP rows for the mixed-vs-FP64 accuracy solve")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the accuracy solve")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------------------- ranks
+class Ranks:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+            self.backend = backend
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.dist:
+            return v
+        import torch
+
+        dev = f"cuda:{self.local}" if self.backend == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi samples during the timed region (every 200 ms)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+def workload_config(a) -> dict:
+    return {"workload": f"incore BN cohort {a.n_ind} x {a.n_snp} (K=8 Dirichlet(1), Fst 0.02, p~U(.01,.5), "
+                        f"2% missing), nrhs {a.nrhs}, one pass X^T X Omega per step",
+            "n_ind": a.n_ind, "n_snp": a.n_snp, "nrhs": a.nrhs, "precision": a.precision,
+            "packed_gb": round(a.n_snp * ((a.n_ind + 3) // 4) / 1e9, 3),
+            "l2": "inputs larger than L2 (packed matrix >> 129 MB); no flush",
+            "parallelism": "replicas (one independent solve per GPU)"}
+
+
+# ----------------------------------------------------------------------------- reference arm
+def reference_arm(a, ranks: Ranks) -> None:
+    if ranks.rank != 0:
+        return
+    from distpca_gb300 import synth
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    c = synth.config_cohort("incore50k", n_snp=a.n_snp, n_ind=a.n_ind)
+    S = min(a.cpu_snps, a.n_snp)
+    sample = O.synth_rows(c, 0, S)
+    om = O.omega(a.n_ind, a.nrhs)
+    walls = []
+    O.one_pass(sample, a.n_ind, om, bsize=min(10_000, S), npasses=a.warmup + a.steps, walls=walls)
+    t = sum(walls[a.warmup:])
+    value = a.n_ind * S * a.steps / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * t / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(a),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{S} SNPs x {a.n_ind} individuals per step (bsize 10000, steady-state "
+                                       f"LUT passes), OpenBLAS {threads} threads, decode single-threaded as in "
+                                       f"the reference"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- dpca arm
+def dominant(kt: dict, prefer: tuple) -> str:
+    cands = {k: v for k, v in kt.items() if v["launches"] > 0}
+    for p in prefer:
+        if p in cands:
+            return max(((k, v) for k, v in cands.items() if k in prefer), key=lambda kv: kv[1]["ms"])[0]
+    return max(cands.items(), key=lambda kv: kv[1]["ms"])[0]
+
+
+def traffic_for(kernel: str):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    except Exception:
+        return None
+
+
+def dpca_arm(a, ranks: Ranks) -> None:
+    import torch
+
+    import distpca_gb300 as D
+    from distpca_gb300 import synth
+
+    dev = ranks.local
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    c = synth.config_cohort("incore50k", n_snp=a.n_snp, n_ind=a.n_ind)
+    prec = D.PREC_MIXED if a.precision == "mixed" else D.PREC_FP64
+    h = D.Handle(a.n_ind, a.n_snp, a.nrhs, precision=prec, device=dev, stream=stream.cuda_stream)
+    h.synth_fill(c)
+    omega = D.start_block(a.n_ind, a.nrhs)
+    h.set_omega(omega)
+    for _ in range(a.warmup):
+        h.pass_()
+    h.synchronize()
+    h.reset_kernel_times(True)
+    clocks = Clocks(dev)
+    ranks.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        h.pass_()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ranks.barrier()
+    ms = e0.elapsed_time(e1)
+    ms_max = ranks.max(ms)
+    kt = h.kernel_times()
+    h.reset_kernel_times(False)
+    launches = int(sum(v["launches"] for v in kt.values()))
+    value = a.n_ind * a.n_snp * a.steps * ranks.world / (ms_max / 1e3)
+    pk = peaks()
+    if a.precision == "mixed":
+        dom = dominant(kt, ("mixed_xw", "mixed_xty"))
+        flops = 2.0 * a.n_snp * a.n_ind * a.nrhs  # algorithmic flops of one product launch
+        avg_s = kt[dom]["ms"] / kt[dom]["launches"] / 1e3
+        roof = {"kernel": dom, "bound": "tensor", "achieved": flops / avg_s / 1e12,
+                "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                "peak_source": f"{pk['source']} bf16 sustained (kernel timed inside a multi-pass loop)"}
+    else:
+        dom = dominant(kt, ("fp64_xw", "fp64_xty"))
+        flops = 2.0 * a.n_snp * a.n_ind * a.nrhs
+        avg_s = kt[dom]["ms"] / kt[dom]["launches"] / 1e3
+        roof = {"kernel": dom, "bound": "fp64", "achieved": flops / avg_s / 1e12, "peak": 1.25, "unit": "TFLOP/s",
+                "peak_source": "nominal FP64 (no measured FP64 peak)"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = traffic_for(dom)
+    roof["algorithmic_per_launch"] = f"{flops:.3e} flop (2 x n_snp x n_ind x nrhs)"
+    kernels = {k: {"ms_per_launch": v["ms"] / max(1, v["launches"]), "launches": v["launches"],
+                   "share": v["ms"] / max(1e-9, sum(x["ms"] for x in kt.values()))} for k, v in kt.items()}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ranks.world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f16 hi+lo x exact 0/1/2, f32 accumulate, f64 dense" if a.precision ==
+            "mixed" else "f64", "data": "synthetic (seeded Balding-Nichols, generated on the device)",
+            "config": workload_config(a), "clocks": clk, "gpu_launches": launches, "roofline": roof,
+            "kernels": kernels}
+    # ---- extras (rank 0, untimed): FP64 GPU comparison, accuracy, e2e, CPU baseline ----
+    host = None
+    np_bytes = (a.n_ind + 3) // 4
+    if ranks.rank == 0 and not (a.no_e2e and a.no_cpu and a.no_extras):
+        host = torch.empty((a.n_snp, np_bytes), dtype=torch.uint8, pin_memory=True)
+        hv = host.numpy()
+        D.lib().dpca_download_packed(h._h, 0, a.n_snp, hv.ctypes.data)
+    h.close()
+    torch.cuda.empty_cache()
+    if ranks.rank == 0 and not a.no_extras and a.precision == "mixed":
+        line["fp64_gpu"] = fp64_comparison(a, hv, value / ranks.world)
+        line["accuracy"] = accuracy_check(a, hv)
+    if ranks.rank == 0 and not a.no_e2e:
+        line["e2e"] = e2e_run(a, hv)
+    if ranks.rank == 0 and not a.no_cpu and ranks.world == 1:
+        line["cpu_baseline"] = cpu_baseline(a, hv)
+    if ranks.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def fp64_comparison(a, hv, mixed_per_gpu: float) -> dict:
+    import torch
+
+    import distpca_gb300 as D
+
+    S = min(a.fp64_snps, a.n_snp)
+    with D.Handle(a.n_ind, S, a.nrhs, precision=D.PREC_FP64, stream=torch.cuda.current_stream().cuda_stream) as h:
+        h.upload_ptr(hv.ctypes.data, hv.shape[1])
+        h.set_omega(D.start_block(a.n_ind, a.nrhs))
+        h.pass_()
+        h.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(2):
+            h.pass_()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 2
+    v = a.n_ind * S / (ms / 1e3)
+    return {"value": v, "unit": UNIT, "sample": f"{S} SNPs x {a.n_ind} individuals, plain FP64 GPU path",
+            "mixed_over_fp64": mixed_per_gpu / v}
+
+
+def accuracy_check(a, hv) -> dict:
+    """Mixed vs plain FP64 on the same start block, same fixed iteration count."""
+    import distpca_gb300 as D
+
+    S = min(a.accuracy_snps, a.n_snp)
+    nsv = a.nrhs // 2
+    sub = hv[:S]
+    kw = dict(nsv=nsv, nrhs=a.nrhs, power=a.power, crit=1, tol=-1.0, miter=1, bsize=10_000, verbose=0)
+    om = D.start_block(a.n_ind, a.nrhs)
+    rm = D.run_packed(sub, a.n_ind, omega0=om, precision="mixed", **kw)
+    rf = D.run_packed(sub, a.n_ind, omega0=om, precision="fp64", **kw)
+    lam_m, lam_f = rm["sigma"] ** 2, rf["sigma"] ** 2
+    qm, _ = np.linalg.qr(rm["u"])
+    qf, _ = np.linalg.qr(rf["u"])
+    s = np.clip(np.linalg.svd(qm.T @ qf, compute_uv=False), -1, 1)
+    corr = np.abs(np.sum(rm["u"] * rf["u"], 0)) / (np.linalg.norm(rm["u"], axis=0) * np.linalg.norm(rf["u"], axis=0))
+    return {"sample": f"{S} SNPs x {a.n_ind}, nrhs {a.nrhs}, nsv {nsv}, power {a.power}, 1 iteration",
+            "eig_rel_err_max": float(np.max(np.abs(lam_m - lam_f) / lam_f)),
+            "principal_angle_max_rad": float(np.arccos(s.min())),
+            "pc_abs_corr_min": float(corr.min())}
+
+
+def e2e_run(a, hv) -> dict:
+    """Through the reference-facing C ABI (dpca_run_packed) from pinned host memory."""
+    import distpca_gb300 as D
+
+    kw = dict(nsv=a.nrhs // 2, nrhs=a.nrhs, power=a.power, crit=1, tol=-1.0, miter=1, bsize=10_000, verbose=0,
+              precision=a.precision)
+    om0 = D.start_block(a.n_ind, a.nrhs)
+    D.run_packed(hv, a.n_ind, omega0=om0, **kw)  # warm-up (context, allocator)
+    times, passes = [], 0
+    for _ in range(a.e2e_steps):
+        t0 = time.perf_counter()
+        r = D.run_packed(hv, a.n_ind, omega0=om0, **kw)
+        times.append(time.perf_counter() - t0)
+        passes = r["passes"]
+    t = sum(times) / len(times)
+    return {"value": a.n_ind * a.n_snp * passes / t, "unit": UNIT,
+            "h2d_bytes_per_step": int(hv.nbytes + a.n_ind * a.nrhs * 8),
+            "d2h_bytes_per_step": int(a.n_ind * a.nrhs * 8),
+            "call": f"dpca_run_packed, 1 outer iteration = {passes} passes incl. H2D, stats, QR, Rayleigh-Ritz",
+            "seconds_per_call": t}
+
+
+def cpu_baseline(a, hv) -> dict:
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    S = min(a.cpu_snps, a.n_snp)
+    om = O.omega(a.n_ind, a.nrhs)
+    walls = []
+    O.one_pass(np.ascontiguousarray(hv[:S]), a.n_ind, om, bsize=min(10_000, S), npasses=2, walls=walls)
+    return {"value": a.n_ind * S / walls[-1], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{S} SNPs x {a.n_ind} individuals, one steady-state pass (bsize 10000), OpenBLAS "
+                      f"{threads} threads"}
+
+
+def main():
+    a = parse()
+    ranks = Ranks()
+    try:
+        if a.impl == "reference":
+            reference_arm(a, ranks)
+        else:
+            dpca_arm(a, ranks)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,148 @@
+// Internal declarations shared by the host (.cpp) and device (.cu) parts of libdpca.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "dpca.h"
+
+namespace dpca {
+
+void set_error(const char *fmt, ...);
+void clear_error();
+
+#define DPCA_TRY(expr)                                 \
+    do {                                               \
+        dpca_status st_ = (expr);                      \
+        if (st_ != DPCA_OK) return st_;                \
+    } while (0)
+
+#define DPCA_CUDA(call)                                                                                  \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            ::dpca::set_error("%s:%d: %s -> %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));     \
+            return e_ == cudaErrorMemoryAllocation ? DPCA_ERR_NOMEM : DPCA_ERR_CUDA;                     \
+        }                                                                                                \
+    } while (0)
+
+// Largest subspace width the device kernels accept (tcgen05 N <= 256 holds 2*nrhs).
+constexpr int kMaxNrhs = 128;
+
+// Per-kernel CUDA-event timing on the handle's stream.
+struct KernelClock {
+    struct Pending {
+        int slot;
+        cudaEvent_t a, b;
+    };
+    bool enabled = false;
+    std::vector<std::string> names;
+    std::vector<double> ms;
+    std::vector<int64_t> launches;
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    int slot(const char *name);
+    cudaEvent_t get_event();
+    void resolve();  // accumulate finished pairs (synchronizes on their end events)
+    void reset();
+    ~KernelClock();
+};
+
+// Scoped timing of one launch: records events around the enclosed launch when enabled.
+struct ScopedLaunch {
+    KernelClock *clk;
+    cudaStream_t st;
+    int slot = -1;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ScopedLaunch(KernelClock *c, cudaStream_t s, const char *name);
+    ~ScopedLaunch();
+};
+
+struct Handle {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int n_ind = 0, n_snp = 0, k = 0, precision = DPCA_PREC_MIXED;
+    int64_t np = 0;       // packed bytes per SNP row = ceil(n_ind/4)
+    int64_t pitch = 0;    // device row pitch of P (multiple of 128 B)
+    int64_t npT = 0;      // packed bytes per individual row of P^T = ceil(n_snp/4)
+    int64_t pitchT = 0;   // device row pitch of P^T
+    int n_ind_pad = 0;    // n_ind rounded up to 128 (operand padding)
+    int n_snp_pad = 0;    // n_snp rounded up to 128
+    double inv_sqrt_nsnp = 0;
+
+    uint8_t *P = nullptr;    // SNP-major packed matrix, n_snp x pitch
+    uint8_t *PT = nullptr;   // individual-major packed matrix (mixed path), n_ind x pitchT
+
+    // per-SNP statistics
+    int32_t *counts = nullptr;  // [n_snp][4] codes 00,01,10,11
+    double *avg = nullptr, *sd = nullptr;
+    double *lut = nullptr;      // [n_snp][4] standardized value per raw code (times 1/sqrt(n_snp))
+    double *coef = nullptr;     // [n_snp][2] mixed path: X = b*g + a*nonmissing -> {b, a}
+    double *rowbound = nullptr; // [n_snp] mixed path: max(|b|,|a|) * ||X_s||_2
+    bool stats_ready = false;
+
+    // dense FP64 state, n_ind x k row-major unless noted
+    double *omega = nullptr, *z = nullptr, *q = nullptr, *old = nullptr, *work = nullptr;
+    double *y = nullptr;        // n_snp x k (X Omega)
+    double *partial = nullptr;  // split-K partials
+    size_t partial_elems = 0;
+    double *small = nullptr;    // k x k matrices, eigenvalues, sigma, scalars (see SmallLayout)
+    double *red = nullptr;      // reduction scratch
+    size_t red_elems = 0;
+    int *dflag = nullptr;       // device error / status flags
+    double *host_small = nullptr; // pinned mirror of small results
+
+    // mixed-precision operands
+    void *mx = nullptr;         // MixedState (k_mixed.cu)
+
+    KernelClock clock;
+};
+
+// Offsets (in doubles) inside Handle::small.
+struct SmallLayout {
+    int k;
+    __host__ __device__ size_t B() const { return 0; }                    // k*k Rayleigh / Gram matrix
+    __host__ __device__ size_t W() const { return (size_t)k * k; }        // k*k eigenvectors (descending)
+    __host__ __device__ size_t w() const { return 2 * (size_t)k * k; }    // k eigenvalues (descending)
+    __host__ __device__ size_t sigma() const { return w() + k; }          // k
+    __host__ __device__ size_t sigma_old() const { return sigma() + k; }  // k
+    __host__ __device__ size_t dots() const { return sigma_old() + k; }   // k MEV dot products
+    __host__ __device__ size_t tau() const { return dots() + k; }         // k Householder scalars
+    __host__ __device__ size_t crit() const { return tau() + k; }         // [0] criterion value, [1] stop flag, [2] sum sigma
+    __host__ __device__ size_t total() const { return crit() + 8; }
+};
+
+// ---- launchers (device code in .cu files); all stream-ordered on h->stream ----
+dpca_status launch_snp_stats(Handle *h);
+dpca_status launch_synth_fill(Handle *h, uint64_t key, const uint8_t *d_pop, const uint32_t *d_miss,
+                              const uint32_t *d_thr, int n_pop);
+dpca_status launch_transpose_packed(Handle *h);
+dpca_status launch_fp64_xw(Handle *h, const double *omega, double *y);
+dpca_status launch_fp64_xty(Handle *h, const double *y, double *z);
+dpca_status launch_qr(Handle *h, double *a);
+dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, double *out);  // k x k = A^T B
+dpca_status launch_eig_desc(Handle *h);                                                   // small.B -> W, w
+dpca_status launch_apply_w(Handle *h, const double *q, double *out);                      // out = Q W
+dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol, int ii, const double *old,
+                                       const double *omega);
+
+// mixed-precision pass (k_mixed.cu)
+dpca_status mixed_prepare(Handle *h);
+dpca_status mixed_release(Handle *h);
+dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out_or_null);
+dpca_status launch_mixed_xty(Handle *h, double *z);
+
+// host-side helpers shared between translation units
+dpca_status handle_pass(Handle *h);
+bool env_flag(const char *name);
+
+}  // namespace dpca
+
+struct dpca_handle {
+    dpca::Handle h;
+};

@@ -1,0 +1,543 @@
+// Device-resident handle: allocation, upload, one pass, and the subspace iteration.
+//
+// The iteration follows BlockSubspaceIter_MPI_OOC_double_buffering (methods.cpp:941-1066):
+//   pass; (QR -> pass) x (power-1); QR -> pass; B = Q^T Z; eig(upper B) descending;
+//   Omega = Q W; sigma_j = sqrt(w_j); criterion for ii > 0;
+// and, when the block size covers every SNP, SubspaceIteration_MPI (methods.cpp:52-258), whose
+// last step is the half pass Y = X Q with the Gram form B = Y^T Y.  Everything runs on the
+// device; the host reads back nsv singular values and the criterion flag once per iteration.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+#include "dpca_internal.h"
+
+namespace dpca {
+
+// ------------------------------------------------------------------ per-kernel clock
+int KernelClock::slot(const char *name) {
+    for (size_t i = 0; i < names.size(); ++i)
+        if (names[i] == name) return (int)i;
+    names.emplace_back(name);
+    ms.push_back(0.0);
+    launches.push_back(0);
+    return (int)names.size() - 1;
+}
+
+cudaEvent_t KernelClock::get_event() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void KernelClock::resolve() {
+    for (auto &p : pending) {
+        float t = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess)
+            ms[p.slot] += t;
+        pool.push_back(p.a);
+        pool.push_back(p.b);
+    }
+    pending.clear();
+}
+
+void KernelClock::reset() {
+    resolve();
+    for (auto &v : ms) v = 0.0;
+    for (auto &v : launches) v = 0;
+}
+
+KernelClock::~KernelClock() {
+    for (auto &p : pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+}
+
+ScopedLaunch::ScopedLaunch(KernelClock *c, cudaStream_t s, const char *name) : clk(c), st(s) {
+    if (!clk || !clk->enabled) return;
+    slot = clk->slot(name);
+    a = clk->get_event();
+    b = clk->get_event();
+    cudaEventRecord(a, st);
+}
+
+ScopedLaunch::~ScopedLaunch() {
+    if (slot < 0) return;
+    cudaEventRecord(b, st);
+    clk->launches[slot]++;
+    clk->pending.push_back({slot, a, b});
+}
+
+bool env_flag(const char *name) {
+    const char *v = getenv(name);
+    return v && *v && strcmp(v, "0") != 0;
+}
+
+static size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
+
+template <typename T>
+static dpca_status dalloc(T **p, size_t elems) {
+    *p = nullptr;
+    if (elems == 0) return DPCA_OK;
+    cudaError_t e = cudaMalloc((void **)p, elems * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc(%zu bytes): %s", elems * sizeof(T), cudaGetErrorString(e));
+        *p = nullptr;
+        return DPCA_ERR_NOMEM;
+    }
+    return DPCA_OK;
+}
+
+static void free_all(Handle *h) {
+    if (h->mx) mixed_release(h);
+    void *ptrs[] = {h->P, h->PT, h->counts, h->avg, h->sd, h->lut, h->coef, h->rowbound, h->omega, h->z, h->q,
+                    h->old, h->work, h->y, h->partial, h->small, h->red, h->dflag};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (h->host_small) cudaFreeHost(h->host_small);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+}
+
+static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int precision, int device, void *stream) {
+    if (n_ind <= 0 || n_snp <= 0 || nrhs <= 0) {
+        set_error("dpca_create: n_ind, n_snp and nrhs must be positive");
+        return DPCA_ERR_INVALID;
+    }
+    if (nrhs > kMaxNrhs) {
+        set_error("dpca_create: nrhs=%d exceeds the device limit %d", nrhs, kMaxNrhs);
+        return DPCA_ERR_UNSUPPORTED;
+    }
+    if (precision != DPCA_PREC_FP64 && precision != DPCA_PREC_MIXED) {
+        set_error("dpca_create: unknown precision %d", precision);
+        return DPCA_ERR_INVALID;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device available (libdpca has no CPU fallback)");
+        return DPCA_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) {
+        set_error("device %d out of range (%d devices)", device, ndev);
+        return DPCA_ERR_INVALID;
+    }
+    DPCA_CUDA(cudaSetDevice(device));
+    h->device = device;
+    DPCA_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
+    if (stream) {
+        h->stream = (cudaStream_t)stream;
+        h->own_stream = false;
+    } else {
+        DPCA_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    h->n_ind = n_ind;
+    h->n_snp = n_snp;
+    h->k = nrhs;
+    h->precision = precision;
+    h->np = (n_ind + 3) / 4;
+    h->pitch = (int64_t)round_up((size_t)h->np, 128);
+    h->npT = (n_snp + 3) / 4;
+    h->pitchT = (int64_t)round_up((size_t)h->npT, 128);
+    h->n_ind_pad = (int)round_up((size_t)n_ind, 128);
+    h->n_snp_pad = (int)round_up((size_t)n_snp, 128);
+    h->inv_sqrt_nsnp = 1.0 / sqrt((double)n_snp);
+    size_t nk = (size_t)n_ind * nrhs;
+    DPCA_TRY(dalloc(&h->P, (size_t)n_snp * h->pitch));
+    DPCA_CUDA(cudaMemsetAsync(h->P, 0, (size_t)n_snp * h->pitch, h->stream));
+    DPCA_TRY(dalloc(&h->counts, 4 * (size_t)n_snp));
+    DPCA_TRY(dalloc(&h->avg, (size_t)n_snp));
+    DPCA_TRY(dalloc(&h->sd, (size_t)n_snp));
+    DPCA_TRY(dalloc(&h->lut, 4 * (size_t)n_snp));
+    DPCA_TRY(dalloc(&h->coef, 2 * (size_t)n_snp));
+    DPCA_TRY(dalloc(&h->rowbound, (size_t)n_snp));
+    DPCA_TRY(dalloc(&h->omega, nk));
+    DPCA_TRY(dalloc(&h->z, nk));
+    DPCA_TRY(dalloc(&h->q, nk));
+    DPCA_TRY(dalloc(&h->old, nk));
+    DPCA_TRY(dalloc(&h->work, nk));
+    DPCA_TRY(dalloc(&h->y, (size_t)n_snp * nrhs));
+    // FP64 split-K partials: up to ceil(4*SMs / tiles) splits
+    {
+        int tiles = (n_ind + 127) / 128;
+        int s = std::max(1, (4 * h->sm_count + tiles - 1) / tiles);
+        s = std::min(s, std::max(1, (n_snp + 31) / 32));
+        h->partial_elems = (size_t)s * nk;
+        DPCA_TRY(dalloc(&h->partial, h->partial_elems));
+    }
+    SmallLayout L{nrhs};
+    DPCA_TRY(dalloc(&h->small, L.total()));
+    DPCA_CUDA(cudaMemsetAsync(h->small, 0, L.total() * sizeof(double), h->stream));
+    h->red_elems = std::max<size_t>({(size_t)2 * h->sm_count * (size_t)nrhs * nrhs,
+                                     (size_t)4 * h->sm_count * (nrhs + 1), (size_t)nrhs * nrhs + 64});
+    DPCA_TRY(dalloc(&h->red, h->red_elems));
+    DPCA_TRY(dalloc(&h->dflag, 16));
+    DPCA_CUDA(cudaMemsetAsync(h->dflag, 0, 16 * sizeof(int), h->stream));
+    DPCA_CUDA(cudaMallocHost((void **)&h->host_small, L.total() * sizeof(double)));
+    if (precision == DPCA_PREC_MIXED) {
+        DPCA_TRY(dalloc(&h->PT, (size_t)n_ind * h->pitchT));
+        DPCA_CUDA(cudaMemsetAsync(h->PT, 0, (size_t)n_ind * h->pitchT, h->stream));
+        DPCA_TRY(mixed_prepare(h));
+    }
+    h->clock.enabled = env_flag("DPCA_KERNEL_CLOCK");
+    return DPCA_OK;
+}
+
+static dpca_status after_data(Handle *h) {
+    DPCA_TRY(launch_snp_stats(h));
+    if (h->precision == DPCA_PREC_MIXED) DPCA_TRY(launch_transpose_packed(h));
+    h->stats_ready = true;
+    return DPCA_OK;
+}
+
+dpca_status handle_pass_io(Handle *h, const double *in, double *out) {
+    if (!h->stats_ready) {
+        set_error("no genotype data on the device (call dpca_upload or dpca_synth_fill)");
+        return DPCA_ERR_INVALID;
+    }
+    if (h->precision == DPCA_PREC_FP64) {
+        DPCA_TRY(launch_fp64_xw(h, in, h->y));
+        DPCA_TRY(launch_fp64_xty(h, h->y, out));
+    } else {
+        DPCA_TRY(launch_mixed_xw(h, in, nullptr));
+        DPCA_TRY(launch_mixed_xty(h, out));
+    }
+    return DPCA_OK;
+}
+
+dpca_status handle_pass(Handle *h) { return handle_pass_io(h, h->omega, h->z); }
+
+// Y = X Q only (the in-core variant's half pass), into h->y as FP64.
+static dpca_status half_pass(Handle *h, const double *in) {
+    if (h->precision == DPCA_PREC_FP64) return launch_fp64_xw(h, in, h->y);
+    return launch_mixed_xw(h, in, h->y);
+}
+
+static double slot_ms(const KernelClock &c, const char *name) {
+    for (size_t i = 0; i < c.names.size(); ++i)
+        if (c.names[i] == name) return c.ms[i];
+    return 0.0;
+}
+
+static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_inout, dpca_result *res) {
+    const int n = h->n_ind, k = h->k;
+    if (!cfg || !omega_inout || !res) {
+        set_error("dpca_solve: null argument");
+        return DPCA_ERR_INVALID;
+    }
+    const int nsv = cfg->nsv, miter = cfg->miter, power = cfg->power, crit = cfg->crit;
+    if (nsv <= 0 || nsv > k) {
+        set_error("dpca_solve: nsv=%d must be in [1, nrhs=%d]", nsv, k);
+        return DPCA_ERR_INVALID;
+    }
+    if (!h->stats_ready) {
+        set_error("no genotype data on the device");
+        return DPCA_ERR_INVALID;
+    }
+    const bool in_core = cfg->bsize >= h->n_snp;
+    const size_t nkb = (size_t)n * k * sizeof(double);
+    SmallLayout L{k};
+    bool clock_was = h->clock.enabled;
+    h->clock.reset();
+    h->clock.enabled = true;
+    cudaEvent_t t0, t1;
+    DPCA_CUDA(cudaEventCreate(&t0));
+    DPCA_CUDA(cudaEventCreate(&t1));
+    DPCA_CUDA(cudaEventRecord(t0, h->stream));
+    DPCA_CUDA(cudaMemcpyAsync(h->omega, omega_inout, nkb, cudaMemcpyHostToDevice, h->stream));
+    DPCA_CUDA(cudaMemsetAsync(h->small, 0, L.total() * sizeof(double), h->stream));
+    if (crit == 2) DPCA_CUDA(cudaMemcpyAsync(h->old, h->omega, nkb, cudaMemcpyDeviceToDevice, h->stream));
+    double *omega = h->omega, *z = h->z, *q = h->q;
+    int ii = 0, passes = 0;
+    bool stopped = false;
+    for (ii = 0; ii < miter; ++ii) {
+        DPCA_TRY(handle_pass_io(h, omega, z));
+        passes++;
+        for (int kk = 0; kk < power - 1; ++kk) {
+            DPCA_TRY(launch_qr(h, z));
+            std::swap(omega, z);  // Omega <- Q
+            DPCA_TRY(handle_pass_io(h, omega, z));
+            passes++;
+        }
+        DPCA_TRY(launch_qr(h, z));
+        std::swap(q, z);  // Q
+        if (in_core) {
+            DPCA_TRY(half_pass(h, q));
+            DPCA_TRY(launch_atb(h, h->y, h->y, h->n_snp, h->small + L.B()));
+        } else {
+            DPCA_TRY(handle_pass_io(h, q, z));
+            passes++;
+            DPCA_TRY(launch_atb(h, q, z, n, h->small + L.B()));
+        }
+        DPCA_TRY(launch_eig_desc(h));
+        DPCA_TRY(launch_apply_w(h, q, omega));
+        DPCA_TRY(launch_sigma_and_criterion(h, nsv, crit, cfg->tol, ii, h->old, omega));
+        DPCA_CUDA(cudaMemcpyAsync(h->host_small, h->small, L.total() * sizeof(double), cudaMemcpyDeviceToHost,
+                                  h->stream));
+        DPCA_CUDA(cudaStreamSynchronize(h->stream));
+        const double *hs = h->host_small;
+        if (res->delta_iter) res->delta_iter[ii] = hs[L.crit() + 2];
+        if (cfg->verbose > 1 && ii > 0) {
+            if (crit == 0) printf("Iteration %d: rel. error: %02.13f\n", ii, hs[L.crit()]);
+            else if (crit == 1) printf("Iteration %d: %d converged\n", ii, (int)hs[L.crit()]);
+            else if (crit == 2) printf("Iteration %d: MEV error: %02.13f\n", ii, hs[L.crit()]);
+        }
+        if (hs[L.crit() + 1] != 0.0) {
+            stopped = true;
+            break;
+        }
+        if (crit == 2) DPCA_CUDA(cudaMemcpyAsync(h->old, omega, nkb, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    DPCA_CUDA(cudaEventRecord(t1, h->stream));
+    DPCA_CUDA(cudaMemcpyAsync(omega_inout, omega, nkb, cudaMemcpyDeviceToHost, h->stream));
+    DPCA_CUDA(cudaStreamSynchronize(h->stream));
+    // keep the handle's canonical buffers pointing at distinct allocations
+    h->omega = omega;
+    h->z = z;
+    h->q = q;
+    float total_ms = 0.f;
+    cudaEventElapsedTime(&total_ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    res->n_ind = n;
+    res->n_snp = h->n_snp;
+    res->nsv = nsv;
+    res->nrhs = k;
+    res->total_its = stopped ? ii + 1 : ii;
+    res->passes = passes;
+    res->in_core = in_core ? 1 : 0;
+    if (res->sigma) memcpy(res->sigma, h->host_small + L.sigma(), (size_t)nsv * sizeof(double));
+    if (res->u)
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < nsv; ++j) res->u[(size_t)i * nsv + j] = omega_inout[(size_t)i * k + j];
+    h->clock.resolve();
+    const KernelClock &c = h->clock;
+    double xw = slot_ms(c, "fp64_xw") + slot_ms(c, "mixed_xw") + slot_ms(c, "split_omega");
+    double xty = slot_ms(c, "fp64_xty") + slot_ms(c, "reduce_splits") + slot_ms(c, "mixed_xty") +
+                 slot_ms(c, "mixed_reduce");
+    res->time_mm_a = xw * 1e-3;
+    res->time_mm_a_t = xty * 1e-3;
+    res->time_mm = (xw + xty + slot_ms(c, "atb") + slot_ms(c, "apply_w")) * 1e-3;
+    res->time_gs = slot_ms(c, "hh_qr") * 1e-3;
+    res->time_projected_svd = slot_ms(c, "jacobi_eig") * 1e-3;
+    res->time_other = total_ms * 1e-3 - res->time_mm - res->time_gs - res->time_projected_svd;
+    if (res->time_other < 0) res->time_other = 0;
+    h->clock.enabled = clock_was;
+    for (int j = 0; j < nsv; ++j)
+        if (!std::isfinite(h->host_small[L.sigma() + j]) && h->host_small[L.w() + j] >= 0) {
+            set_error("non-finite singular value %d", j);
+            return DPCA_ERR_NUMERIC;
+        }
+    return DPCA_OK;
+}
+
+}  // namespace dpca
+
+using namespace dpca;
+
+extern "C" {
+
+dpca_status dpca_create(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device, void *stream) {
+    clear_error();
+    if (!out) return DPCA_ERR_INVALID;
+    *out = nullptr;
+    dpca_handle *hh = new (std::nothrow) dpca_handle();
+    if (!hh) return DPCA_ERR_NOMEM;
+    dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream);
+    if (st != DPCA_OK) {
+        free_all(&hh->h);
+        delete hh;
+        return st;
+    }
+    *out = hh;
+    return DPCA_OK;
+}
+
+dpca_status dpca_destroy(dpca_handle *hh) {
+    if (!hh) return DPCA_OK;
+    cudaSetDevice(hh->h.device);
+    if (hh->h.stream) cudaStreamSynchronize(hh->h.stream);
+    free_all(&hh->h);
+    delete hh;
+    return DPCA_OK;
+}
+
+dpca_status dpca_upload(dpca_handle *hh, const uint8_t *packed, int64_t row_stride) {
+    clear_error();
+    if (!hh || !packed) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    if (row_stride < h->np) {
+        set_error("row_stride %lld < ceil(n_ind/4) = %lld", (long long)row_stride, (long long)h->np);
+        return DPCA_ERR_INVALID;
+    }
+    DPCA_CUDA(cudaSetDevice(h->device));
+    {
+        ScopedLaunch t(&h->clock, h->stream, "h2d_packed");
+        // chunked 2D copies keep each transfer bounded
+        const int64_t rows_per = std::max<int64_t>(1, (int64_t)(256 << 20) / std::max<int64_t>(1, row_stride));
+        for (int64_t s0 = 0; s0 < h->n_snp; s0 += rows_per) {
+            int64_t rows = std::min<int64_t>(rows_per, h->n_snp - s0);
+            DPCA_CUDA(cudaMemcpy2DAsync(h->P + s0 * h->pitch, h->pitch, packed + s0 * row_stride, row_stride, h->np,
+                                        rows, cudaMemcpyHostToDevice, h->stream));
+        }
+    }
+    DPCA_TRY(after_data(h));
+    return DPCA_OK;
+}
+
+dpca_status dpca_synth_fill(dpca_handle *hh, uint64_t key, const uint8_t *pop, const uint32_t *miss_thr,
+                            const uint32_t *snp_thr, int n_pop) {
+    clear_error();
+    if (!hh || !pop || !miss_thr || !snp_thr || n_pop <= 0) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    DPCA_CUDA(cudaSetDevice(h->device));
+    uint8_t *d_pop = nullptr;
+    uint32_t *d_miss = nullptr, *d_thr = nullptr;
+    DPCA_TRY(dalloc(&d_pop, (size_t)h->n_ind));
+    DPCA_TRY(dalloc(&d_miss, (size_t)h->n_ind));
+    DPCA_TRY(dalloc(&d_thr, (size_t)h->n_snp * n_pop));
+    DPCA_CUDA(cudaMemcpyAsync(d_pop, pop, (size_t)h->n_ind, cudaMemcpyHostToDevice, h->stream));
+    DPCA_CUDA(cudaMemcpyAsync(d_miss, miss_thr, (size_t)h->n_ind * 4, cudaMemcpyHostToDevice, h->stream));
+    DPCA_CUDA(cudaMemcpyAsync(d_thr, snp_thr, (size_t)h->n_snp * n_pop * 4, cudaMemcpyHostToDevice, h->stream));
+    dpca_status st = launch_synth_fill(h, key, d_pop, d_miss, d_thr, n_pop);
+    cudaStreamSynchronize(h->stream);
+    cudaFree(d_pop);
+    cudaFree(d_miss);
+    cudaFree(d_thr);
+    DPCA_TRY(st);
+    DPCA_TRY(after_data(h));
+    return DPCA_OK;
+}
+
+dpca_status dpca_download_packed(dpca_handle *hh, int s0, int s1, uint8_t *out) {
+    clear_error();
+    if (!hh || !out) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    if (s0 < 0 || s1 > h->n_snp || s0 > s1) {
+        set_error("SNP range [%d, %d) outside [0, %d)", s0, s1, h->n_snp);
+        return DPCA_ERR_INVALID;
+    }
+    DPCA_CUDA(cudaSetDevice(h->device));
+    if (s1 > s0)
+        DPCA_CUDA(cudaMemcpy2DAsync(out, h->np, h->P + (int64_t)s0 * h->pitch, h->pitch, h->np, s1 - s0,
+                                    cudaMemcpyDeviceToHost, h->stream));
+    DPCA_CUDA(cudaStreamSynchronize(h->stream));
+    return DPCA_OK;
+}
+
+dpca_status dpca_snp_stats(dpca_handle *hh, int32_t *counts, double *avg, double *sd, double *lut) {
+    clear_error();
+    if (!hh) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    if (!h->stats_ready) {
+        set_error("no genotype data on the device");
+        return DPCA_ERR_INVALID;
+    }
+    DPCA_CUDA(cudaSetDevice(h->device));
+    size_t n = (size_t)h->n_snp;
+    if (counts) DPCA_CUDA(cudaMemcpyAsync(counts, h->counts, 4 * n * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (avg) DPCA_CUDA(cudaMemcpyAsync(avg, h->avg, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (sd) DPCA_CUDA(cudaMemcpyAsync(sd, h->sd, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (lut) DPCA_CUDA(cudaMemcpyAsync(lut, h->lut, 4 * n * 8, cudaMemcpyDeviceToHost, h->stream));
+    DPCA_CUDA(cudaStreamSynchronize(h->stream));
+    return DPCA_OK;
+}
+
+dpca_status dpca_set_omega(dpca_handle *hh, const double *omega) {
+    clear_error();
+    if (!hh || !omega) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    DPCA_CUDA(cudaSetDevice(h->device));
+    DPCA_CUDA(cudaMemcpyAsync(h->omega, omega, (size_t)h->n_ind * h->k * 8, cudaMemcpyHostToDevice, h->stream));
+    return DPCA_OK;
+}
+
+dpca_status dpca_pass(dpca_handle *hh) {
+    clear_error();
+    if (!hh) return DPCA_ERR_INVALID;
+    DPCA_CUDA(cudaSetDevice(hh->h.device));
+    return handle_pass(&hh->h);
+}
+
+dpca_status dpca_get_z(dpca_handle *hh, double *z) {
+    clear_error();
+    if (!hh || !z) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    DPCA_CUDA(cudaSetDevice(h->device));
+    DPCA_CUDA(cudaMemcpyAsync(z, h->z, (size_t)h->n_ind * h->k * 8, cudaMemcpyDeviceToHost, h->stream));
+    DPCA_CUDA(cudaStreamSynchronize(h->stream));
+    return DPCA_OK;
+}
+
+dpca_status dpca_solve(dpca_handle *hh, const dpca_config *cfg, double *omega_inout, dpca_result *res) {
+    clear_error();
+    if (!hh) return DPCA_ERR_INVALID;
+    DPCA_CUDA(cudaSetDevice(hh->h.device));
+    return solve_impl(&hh->h, cfg, omega_inout, res);
+}
+
+dpca_status dpca_synchronize(dpca_handle *hh) {
+    clear_error();
+    if (!hh) return DPCA_ERR_INVALID;
+    DPCA_CUDA(cudaStreamSynchronize(hh->h.stream));
+    int flags[4] = {0, 0, 0, 0};
+    DPCA_CUDA(cudaMemcpy(flags, hh->h.dflag, sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags[0]) {
+        set_error("device wait gave up (code %d, stage %d)", flags[0], flags[1]);
+        return DPCA_ERR_TIMEOUT;
+    }
+    return DPCA_OK;
+}
+
+dpca_status dpca_kernel_times(dpca_handle *hh, char *names, size_t cap_names, double *ms, int64_t *launches,
+                              int *count, int cap) {
+    clear_error();
+    if (!hh || !count) return DPCA_ERR_INVALID;
+    KernelClock &c = hh->h.clock;
+    c.resolve();
+    int n = (int)c.names.size();
+    *count = n;
+    std::string joined;
+    for (int i = 0; i < n; ++i) {
+        if (i) joined += ';';
+        joined += c.names[i];
+        if (i < cap) {
+            if (ms) ms[i] = c.ms[i];
+            if (launches) launches[i] = c.launches[i];
+        }
+    }
+    if (names && cap_names) {
+        strncpy(names, joined.c_str(), cap_names - 1);
+        names[cap_names - 1] = 0;
+    }
+    return DPCA_OK;
+}
+
+dpca_status dpca_reset_kernel_times(dpca_handle *hh, int enable) {
+    clear_error();
+    if (!hh) return DPCA_ERR_INVALID;
+    hh->h.clock.reset();
+    hh->h.clock.enabled = enable != 0;
+    return DPCA_OK;
+}
+
+dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp, int32_t *counts,
+                               double *avg, double *sd) {
+    clear_error();
+    dpca_handle *hh = nullptr;
+    DPCA_TRY(dpca_create(&hh, n_ind, n_snp, 1, DPCA_PREC_FP64, 0, nullptr));
+    dpca_status st = dpca_upload(hh, packed, row_stride);
+    if (st == DPCA_OK) st = dpca_snp_stats(hh, counts, avg, sd, nullptr);
+    dpca_destroy(hh);
+    return st;
+}
+
+}  // extern "C"

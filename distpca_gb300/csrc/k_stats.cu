@@ -1,0 +1,191 @@
+// Per-SNP decode statistics, the synthetic-cohort fill, and the individual-major
+// transposed copy of the packed matrix.
+//
+// snp_stats_kernel restates, on the device and bit-exactly,
+//   decode_plink_sse2 (utilities.cpp:351-414): code 00 -> 0, 01 -> missing, 10 -> 1, 11 -> 2;
+//   standardize (utilities.cpp:272-292): avg = sum/ctr over non-missing, p = avg/2,
+//     sd = sqrt(2p(1-p)) -- all in IEEE FP64 with explicit round-to-nearest ops so that no
+//     contraction can change a bit;
+//   the LUT cache (methods.cpp:819-843): value per code = ((g - avg)/sd) * (1/sqrt(n_snp)),
+//     zero for missing codes and for SNPs with sd <= 1e-9.
+// Counting is a popcount over 16 codes per 32-bit word with 128-bit coalesced loads; one warp
+// owns one SNP row and reduces its four counts with shuffles.
+#include "common.cuh"
+#include "dpca_internal.h"
+
+namespace dpca {
+
+__global__ void __launch_bounds__(256) snp_stats_kernel(const uint8_t *__restrict__ P, int64_t pitch, int n_ind,
+                                                        int n_snp, int64_t np, double inv_sqrt_nsnp,
+                                                        int32_t *__restrict__ counts, double *__restrict__ avg,
+                                                        double *__restrict__ sd, double *__restrict__ lut,
+                                                        double *__restrict__ coef, double *__restrict__ rowbound) {
+    int lane = threadIdx.x & 31;
+    int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (s >= n_snp) return;
+    const uint4 *row = reinterpret_cast<const uint4 *>(P + s * pitch);
+    int nchunk = (int)((np + 15) >> 4);
+    int c00 = 0, c01 = 0, c10 = 0, c11 = 0;
+#pragma unroll 4
+    for (int c = lane; c < nchunk; c += 32) {
+        uint4 v = __ldg(row + c);
+        uint32_t ws[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int base = c * 64 + j * 16;  // first individual of this word
+            int valid = n_ind - base;
+            uint32_t m = valid >= 16 ? 0x55555555u : (valid <= 0 ? 0u : (((1u << (2 * valid)) - 1u) & 0x55555555u));
+            uint32_t hi = (ws[j] >> 1) & m, lo = ws[j] & m;
+            c11 += __popc(hi & lo);
+            c10 += __popc(hi & ~lo);
+            c01 += __popc(~hi & lo);
+            c00 += __popc(m & ~hi & ~lo);
+        }
+    }
+    c00 = warp_sum_int(c00);
+    c01 = warp_sum_int(c01);
+    c10 = warp_sum_int(c10);
+    c11 = warp_sum_int(c11);
+    if (lane != 0) return;
+    counts[4 * s + 0] = c00;
+    counts[4 * s + 1] = c01;
+    counts[4 * s + 2] = c10;
+    counts[4 * s + 3] = c11;
+    double sum = (double)c10 + 2.0 * (double)c11;  // exact: small integers
+    unsigned int ctr = (unsigned int)(c00 + c10 + c11);
+    double mean = __ddiv_rn(sum, (double)ctr);
+    double p = __ddiv_rn(mean, 2.0);
+    double sdev = __dsqrt_rn(__dmul_rn(__dmul_rn(2.0, p), __dsub_rn(1.0, p)));
+    avg[s] = mean;
+    sd[s] = sdev;
+    double v00 = 0.0, v10 = 0.0, v11 = 0.0, b = 0.0, a = 0.0, rb = 0.0;
+    if (sdev > 1e-9) {
+        v00 = __dmul_rn(__ddiv_rn(__dsub_rn(0.0, mean), sdev), inv_sqrt_nsnp);
+        v10 = __dmul_rn(__ddiv_rn(__dsub_rn(1.0, mean), sdev), inv_sqrt_nsnp);
+        v11 = __dmul_rn(__ddiv_rn(__dsub_rn(2.0, mean), sdev), inv_sqrt_nsnp);
+        b = inv_sqrt_nsnp / sdev;
+        a = -mean * b;
+        double nrm = sqrt((double)c00 * v00 * v00 + (double)c10 * v10 * v10 + (double)c11 * v11 * v11);
+        rb = fmax(fabs(a), fabs(b)) * nrm;
+    }
+    lut[4 * s + 0] = v00;
+    lut[4 * s + 1] = 0.0;
+    lut[4 * s + 2] = v10;
+    lut[4 * s + 3] = v11;
+    if (coef) {
+        coef[2 * s + 0] = b;
+        coef[2 * s + 1] = a;
+    }
+    if (rowbound) rowbound[s] = rb;
+}
+
+dpca_status launch_snp_stats(Handle *h) {
+    ScopedLaunch t(&h->clock, h->stream, "snp_stats");
+    int warps_per_block = 8;
+    int grid = ceil_div(h->n_snp, warps_per_block);
+    snp_stats_kernel<<<grid, 32 * warps_per_block, 0, h->stream>>>(h->P, h->pitch, h->n_ind, h->n_snp, h->np,
+                                                                     h->inv_sqrt_nsnp, h->counts, h->avg, h->sd,
+                                                                     h->lut, h->coef, h->rowbound);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
+// One thread writes one 32-bit word (16 individuals) of one SNP row; the
+// genotype of (snp s, individual i) is a pure function of (key, s, i), as in
+// distpca_gb300/synth.py::genotype_codes.
+__global__ void __launch_bounds__(256) synth_fill_kernel(uint8_t *__restrict__ P, int64_t pitch, int n_ind,
+                                                         int n_snp, int64_t words_per_row, uint64_t key,
+                                                         const uint8_t *__restrict__ pop,
+                                                         const uint32_t *__restrict__ miss_thr,
+                                                         const uint32_t *__restrict__ thr, int n_pop) {
+    int64_t total = words_per_row * (int64_t)n_snp;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = t / words_per_row;
+        int64_t w = t - s * words_per_row;
+        const uint32_t *ts = thr + s * n_pop;
+        uint32_t word = 0;
+#pragma unroll 4
+        for (int j = 0; j < 16; ++j) {
+            int64_t i = w * 16 + j;
+            if (i >= n_ind) break;
+            uint64_t x = (((uint64_t)s) << 32 | (uint64_t)i) ^ key;
+            uint64_t hg = fmix64(x + kGold);
+            uint64_t hm = fmix64(x ^ kMissSalt);
+            uint32_t th = __ldg(ts + __ldg(pop + i));
+            uint32_t g = ((uint32_t)hg < th ? 1u : 0u) + ((uint32_t)(hg >> 32) < th ? 1u : 0u);
+            uint32_t code = g == 0 ? 0u : (g == 1 ? 2u : 3u);
+            if ((uint32_t)hm < __ldg(miss_thr + i)) code = 1u;
+            word |= code << (2 * j);
+        }
+        *reinterpret_cast<uint32_t *>(P + s * pitch + 4 * w) = word;
+    }
+}
+
+dpca_status launch_synth_fill(Handle *h, uint64_t key, const uint8_t *d_pop, const uint32_t *d_miss,
+                              const uint32_t *d_thr, int n_pop) {
+    int64_t wpr = (h->np + 3) / 4;
+    int64_t total = wpr * h->n_snp;
+    int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 32);
+    synth_fill_kernel<<<grid, 256, 0, h->stream>>>(h->P, h->pitch, h->n_ind, h->n_snp, wpr, key, d_pop, d_miss,
+                                                    d_thr, n_pop);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
+// Individual-major copy: PT[i][s/4] holds the codes of SNPs s..s+3 of individual i (low bits
+// first), the same 2-bit codes as P.  A block transposes a tile of 64 SNPs x 256 individuals
+// through shared memory (one byte per code), reading 64 B per SNP row and writing 16 B per
+// individual row.
+constexpr int kTS = 64;   // SNPs per tile
+constexpr int kTI = 256;  // individuals per tile
+
+__global__ void __launch_bounds__(256) transpose_packed_kernel(const uint8_t *__restrict__ P, int64_t pitch,
+                                                               uint8_t *__restrict__ PT, int64_t pitchT, int n_ind,
+                                                               int n_snp) {
+    __shared__ uint8_t codes[kTS][kTI + 4];
+    int s0 = blockIdx.y * kTS, i0 = blockIdx.x * kTI;
+    int tid = threadIdx.x;
+    // load: 64 rows x 64 bytes; thread -> (row, 16-byte chunk): 256 threads = 64 rows x 4 chunks
+    {
+        int r = tid >> 2, ch = tid & 3;
+        int s = s0 + r;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        int64_t byte0 = (int64_t)(i0 >> 2) + ch * 16;
+        if (s < n_snp && byte0 < pitch) v = *reinterpret_cast<const uint4 *>(P + (int64_t)s * pitch + byte0);
+        uint32_t ws[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 16; ++q) codes[r][ch * 64 + j * 16 + q] = (uint8_t)((ws[j] >> (2 * q)) & 3u);
+    }
+    __syncthreads();
+    // store: 256 individual rows x 16 bytes (64 SNPs); thread -> one individual row
+    int i = i0 + tid;
+    if (i < n_ind) {
+        uint32_t out[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            uint32_t w = 0;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                int s = s0 + j * 16 + q;
+                uint32_t c = s < n_snp ? (uint32_t)codes[j * 16 + q][tid] : 0u;
+                w |= c << (2 * q);
+            }
+            out[j] = w;
+        }
+        int64_t byte0 = (int64_t)(s0 >> 2);
+        *reinterpret_cast<uint4 *>(PT + (int64_t)i * pitchT + byte0) = make_uint4(out[0], out[1], out[2], out[3]);
+    }
+}
+
+dpca_status launch_transpose_packed(Handle *h) {
+    ScopedLaunch t(&h->clock, h->stream, "transpose_packed");
+    dim3 grid(ceil_div(h->n_ind, kTI), ceil_div(h->n_snp, kTS));
+    transpose_packed_kernel<<<grid, 256, 0, h->stream>>>(h->P, h->pitch, h->PT, h->pitchT, h->n_ind, h->n_snp);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
+}  // namespace dpca

@@ -1,0 +1,159 @@
+/*
+ * dpca.h -- C ABI of libdpca, a GB300-native (sm_103a) drop-in for DistPCA's
+ * randomized subspace-iteration PCA on PLINK SNP-major .bed genotypes.
+ *
+ * Conventions
+ *   - Every entry point returns dpca_status; nothing calls exit().  The text
+ *     of the last failure on the calling thread is in dpca_last_error().
+ *   - Host buffers are caller-owned.  Device state hangs off an opaque
+ *     dpca_handle that one host thread drives; work is ordered on one CUDA
+ *     stream (the handle's own, or one the caller passes in).
+ *   - Matrices are row-major.  n_ind = individuals (.fam rows, the
+ *     reference's M), n_snp = markers (.bim rows, the reference's N),
+ *     nrhs = subspace width k.  Omega and the Ritz block are n_ind x nrhs.
+ *   - There is no CPU fallback: entry points that compute need a CUDA
+ *     device and return DPCA_ERR_CUDA when none is usable.
+ *
+ * Reference interfaces replaced (paths relative to the DistPCA checkout):
+ *   dpca_run / dpca_run_packed / dpca_solve
+ *       BlockSubspaceIter_MPI_OOC_double_buffering  src/methods.h:49, src/methods.cpp:702
+ *       SubspaceIteration_MPI (bsize >= n_snp)      src/methods.h:48, src/methods.cpp:24
+ *   dpca_pass
+ *       the pass lambda _compute_matvec_buff         src/methods.cpp:786-936
+ *   dpca_snp_stats / dpca_decode_counts
+ *       decode_plink_sse2 + standardize + LUT cache  src/utilities.cpp:272-306, 351-480;
+ *                                                    src/methods.cpp:819-843
+ *   dpca_start_block
+ *       start-block RNG loop                         src/distpca.cpp:384-394, src/gennorm.c:21-72
+ *   dpca_config_init / dpca_parse_args / dpca_resolve_config
+ *       initialize_structure, findarg, main's clamps src/utilities.cpp:195-232, src/io.c:24-67,
+ *                                                    src/distpca.cpp:83-352
+ *   dpca_probe_bfile
+ *       .fam/.bim line counting                      src/distpca.cpp:102-189
+ *   dpca_write_outputs / dpca_print_statistics
+ *       -fwrite writer and statistics block          src/methods.cpp:1077-1118, src/utilities.cpp:147-193
+ */
+#ifndef DPCA_H
+#define DPCA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DPCA_OK = 0,
+    DPCA_ERR_INVALID = 1,     /* bad argument or inconsistent sizes */
+    DPCA_ERR_IO = 2,          /* file missing, unreadable or short */
+    DPCA_ERR_FORMAT = 3,      /* .bed magic/mode wrong or size does not match .fam/.bim */
+    DPCA_ERR_CUDA = 4,        /* CUDA runtime/driver error or no device */
+    DPCA_ERR_NOMEM = 5,       /* host or device allocation failed */
+    DPCA_ERR_UNSUPPORTED = 6, /* shape outside the kernels' limits (e.g. nrhs > 128) */
+    DPCA_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up */
+    DPCA_ERR_NUMERIC = 8      /* non-finite values in the iteration */
+} dpca_status;
+
+typedef enum {
+    DPCA_PREC_FP64 = 0,  /* plain path: FP64 standardized values, FP64 products */
+    DPCA_PREC_MIXED = 1  /* exact 0/1/2 genotypes x hi+lo FP16 operands on tcgen05, FP32 accumulate */
+} dpca_precision;
+
+/* Run configuration: the DistPCA.exe flags plus device knobs. */
+typedef struct {
+    int nsv;           /* -nsv     sought PCs (default 10) */
+    int nrhs;          /* -nrhs    subspace width (default 20) */
+    int power;         /* -power   passes per outer iteration minus one (default 1) */
+    int crit;          /* -crit    0 trace, 1 per-sigma (default), 2 MEV */
+    int miter;         /* -miter   outer iterations (default 100) */
+    int bsize;         /* -bsize   SNPs per block; <= 0 picks one from -memory/RAM like the reference */
+    int verbose;       /* -verbose (default 1) */
+    int fwrite;        /* -fwrite  write the two result files (default 0) */
+    int full_svd;      /* -fullSVD accuracy check against a dense SVD (default 0) */
+    double tol;        /* -tol     (default 1e-3) */
+    double memory_gb;  /* -memory  host memory budget used by the block-size rule (0 = RAM/10) */
+    char prefix[1024]; /* -prefix  output prefix (default "noprefix") */
+    int precision;     /* dpca_precision (default DPCA_PREC_MIXED) */
+    int device;        /* CUDA device ordinal (default 0) */
+    double hbm_budget_gb; /* packed bytes above this are streamed from pinned host memory (0 = auto) */
+} dpca_config;
+
+/* Results and the reference's timers (seconds).  sigma and u are caller-owned. */
+typedef struct {
+    int n_ind, n_snp, nsv, nrhs;
+    int rows_fetched;   /* block size after the reference's clamps */
+    int total_its;      /* outer iterations performed */
+    int passes;         /* applications of X^T X */
+    int in_core;        /* 1 when the in-core variant's Gram-form Rayleigh quotient was used */
+    int streamed;       /* 1 when packed blocks were streamed from host memory each pass */
+    double *sigma;      /* [nsv]            singular values (sqrt of Ritz values) */
+    double *u;          /* [n_ind * nsv]    left singular vectors, row-major */
+    double *delta_iter; /* [miter] or NULL  sum of sigma per iteration */
+    double time_generate_rhs, time_load_matrix, time_mm, time_mm_a, time_mm_a_t;
+    double time_gs, time_projected_svd, time_other, time_total;
+} dpca_result;
+
+typedef struct dpca_handle dpca_handle;
+
+/* ---- host-side configuration (no device needed) ---- */
+const char *dpca_status_string(dpca_status s);
+const char *dpca_last_error(void);
+const char *dpca_version(void);
+void dpca_config_init(dpca_config *cfg);
+/* findarg semantics: "-name value", first match wins, atoi/atof. bfile gets -bfile. */
+dpca_status dpca_parse_args(int argc, char **argv, dpca_config *cfg, char *bfile, size_t bfile_cap);
+/* n_ind/n_snp from .fam/.bim line counts; checks .bed exists, magic 6C 1B 01 and size. */
+dpca_status dpca_probe_bfile(const char *bfile, int *n_ind, int *n_snp);
+/* The reference's clamps on nsv/nrhs/bsize (distpca.cpp:239-352); writes the final block size. */
+dpca_status dpca_resolve_config(dpca_config *cfg, int n_ind, int n_snp, int *rows_fetched);
+/* Start block, bit-identical to the reference RNG loop: n_ind x k row-major. */
+dpca_status dpca_start_block(int n_ind, int k, double *out);
+
+/* ---- whole runs (device) ---- */
+/* Read <bfile>.bed/.bim/.fam and run.  omega_inout: start block in, final Ritz block out. */
+dpca_status dpca_run(const dpca_config *cfg, const char *bfile, double *omega_inout, dpca_result *res);
+/* Same from packed rows already in host memory (row_stride bytes apart, >= ceil(n_ind/4)). */
+dpca_status dpca_run_packed(const dpca_config *cfg, const uint8_t *packed, int64_t row_stride, int n_ind,
+                            int n_snp, double *omega_inout, dpca_result *res);
+/* Write <prefix>_singularValues.txt and <prefix>_leftSingularVectors.txt (IIDs from <bfile>.fam). */
+dpca_status dpca_write_outputs(const dpca_config *cfg, const char *bfile, const dpca_result *res);
+void dpca_print_statistics(const dpca_config *cfg, const dpca_result *res);
+
+/* ---- device-resident handle ---- */
+/* stream: a cudaStream_t to order work on, or NULL for a handle-owned stream. */
+dpca_status dpca_create(dpca_handle **h, int n_ind, int n_snp, int nrhs, int precision, int device, void *stream);
+dpca_status dpca_destroy(dpca_handle *h);
+/* Copy packed rows (host, pinned or pageable) to the device and compute per-SNP statistics. */
+dpca_status dpca_upload(dpca_handle *h, const uint8_t *packed, int64_t row_stride);
+/* Fill the device matrix with a seeded Balding-Nichols cohort (tables as in distpca_gb300/synth.py):
+ * pop[n_ind] uint8, miss_thr[n_ind] uint32, snp_thr[n_snp * n_pop] uint32 (host arrays). */
+dpca_status dpca_synth_fill(dpca_handle *h, uint64_t key, const uint8_t *pop, const uint32_t *miss_thr,
+                            const uint32_t *snp_thr, int n_pop);
+/* Download packed rows [s0, s1) (row-major, ceil(n_ind/4) bytes per row). */
+dpca_status dpca_download_packed(dpca_handle *h, int s0, int s1, uint8_t *out);
+/* Per-SNP statistics: counts[4*n_snp] = {hom A1 (00), missing (01), het (10), hom A2 (11)},
+ * avg/sd as standardize() computes them, lut[4*n_snp] = standardized value per raw code. */
+dpca_status dpca_snp_stats(dpca_handle *h, int32_t *counts, double *avg, double *sd, double *lut);
+dpca_status dpca_set_omega(dpca_handle *h, const double *omega);
+/* One pass Z = X^T X Omega on the device, stream-ordered (no host sync). */
+dpca_status dpca_pass(dpca_handle *h);
+dpca_status dpca_get_z(dpca_handle *h, double *z);
+/* Full solve on the resident matrix. */
+dpca_status dpca_solve(dpca_handle *h, const dpca_config *cfg, double *omega_inout, dpca_result *res);
+dpca_status dpca_synchronize(dpca_handle *h);
+/* Per-kernel device time (ms) and launch counts accumulated since the last reset, via CUDA events
+ * recorded on the handle's stream around each launch.  names: ';'-separated list. */
+dpca_status dpca_kernel_times(dpca_handle *h, char *names, size_t names_cap, double *ms, int64_t *launches,
+                              int *count, int cap);
+dpca_status dpca_reset_kernel_times(dpca_handle *h, int enable);
+
+/* ---- unit-parity entry: decode + counts for packed rows in host memory ---- */
+dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp, int32_t *counts,
+                               double *avg, double *sd);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DPCA_H */

@@ -1,0 +1,172 @@
+"""Host-side logic of libdpca and its C ABI (no GPU compute).
+
+Covers: every symbol declared in include/dpca.h is exported; the start block
+is bit-identical to the reference's; flag parsing follows findarg; the
+nsv/nrhs/bsize clamps follow distpca.cpp; file probing and its error paths;
+the -fwrite writers and the statistics block use the reference's formats.
+"""
+import ctypes
+import hashlib
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, fileset
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "dpca.h")) as f:
+        text = f.read()
+    # function declarations: a return type at the start of a line, then the name and "("
+    return sorted(set(re.findall(r"^(?:const\s+)?\w+\s*\*?\s*(dpca_[a-z_0-9]+)\s*\(", text, re.M)))
+
+
+def test_header_symbols_exported(dpca):
+    lib = ctypes.CDLL(dpca.library_path())
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(declared_symbols()) == set(dpca.exported_symbols())
+
+
+@pytest.mark.parametrize("n,k", [(37, 6), (203, 10), (1001, 20), (50000, 2)])
+def test_start_block_matches_reference(dpca, golden, n, k):
+    om = dpca.start_block(n, k)
+    assert hashlib.sha256(om.tobytes()).hexdigest() == str(golden[f"omega_{n}x{k}_sha"])
+    if n > 46340:
+        np.testing.assert_array_equal(om[42945:42955], golden[f"omega_{n}x{k}_wrap"])
+
+
+def test_defaults_follow_code_not_readme(dpca):
+    c = dpca.config()
+    assert (c.nsv, c.nrhs, c.power, c.crit, c.miter, c.verbose, c.fwrite) == (10, 20, 1, 1, 100, 1, 0)
+    assert c.tol == 1e-3 and c.prefix == b"noprefix" and c.bsize == 0
+
+
+def test_findarg_semantics(dpca):
+    c, b = dpca.parse_args(["DistPCA.exe", "-bfile", "data/x", "-nsv", "7", "-nsv", "9", "-tol", "1e-6",
+                            "-crit", "2", "-prefix", "out", "-power"])
+    assert b == "data/x"
+    assert c.nsv == 7  # first match wins
+    assert c.tol == 1e-6 and c.crit == 2 and c.prefix == b"out"
+    assert c.power == 1  # flag without value keeps the default
+    c, _ = dpca.parse_args(["x", "-nrhs", "abc"])
+    assert c.nrhs == 0  # atoi("abc")
+    with pytest.raises(dpca.DpcaError):
+        dpca.parse_args(["x", "-precision", "fp8"])
+
+
+@pytest.mark.parametrize("nsv,nrhs,M,N,exp", [
+    (10, 20, 100, 1000, (10, 20)),
+    (40, 5, 37, 300, (37, 37)),      # nsv clamps to min(M,N); nrhs < nsv -> min(2 nsv, min)
+    (5, 0, 100, 1000, (5, 10)),      # nrhs <= 0 -> min(2 nsv, min(M,N))
+    (5, 500, 100, 1000, (5, 100)),   # nrhs > min(M,N) -> min(M,N)
+    (8, 6, 100, 1000, (8, 16)),      # nrhs < nsv
+])
+def test_resolve_clamps(dpca, nsv, nrhs, M, N, exp):
+    c = dpca.config(nsv=nsv, nrhs=nrhs, bsize=50)
+    rows = dpca.resolve(c, M, N)
+    assert (c.nsv, c.nrhs) == exp and rows == 50
+
+
+def test_resolve_block_size_rules(dpca):
+    c = dpca.config(bsize=5000)
+    assert dpca.resolve(c, 100, 1000) == 1000  # > local_N -> local_N (in-core)
+    c = dpca.config(bsize=0, memory=1e-9)  # no memory to spare -> formula of distpca.cpp:259-260
+    rows = dpca.resolve(c, 1000, 100000)
+    membuff = 3.0 * 100000 * 8 + 1000 * 10 * 8 + 2.0 * 100000 * 20 + 3.0 * 1000 * 8 + 2048.0 * 100000
+    assert rows == int((membuff + 1000 * 8.0) / 1e7)
+    c = dpca.config(bsize=0, memory=2.0)
+    rows = dpca.resolve(c, 1000, 100000)
+    assert rows == 100000  # 2 GB fits the whole matrix -> in-core
+    with pytest.raises(dpca.DpcaError):
+        dpca.resolve(dpca.config(nsv=0), 10, 10)
+
+
+def test_probe_counts_and_errors(dpca, tmp_path):
+    prefix = os.path.join(GOLDEN, "small")
+    assert dpca.probe(prefix) == (203, 2500)
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.probe(str(tmp_path / "missing"))
+    assert e.value.status == 2
+    # bad magic
+    p = str(tmp_path / "bad")
+    for ext in (".bim", ".fam"):
+        with open(prefix + ext) as f, open(p + ext, "w") as g:
+            g.write(f.read())
+    with open(prefix + ".bed", "rb") as f:
+        raw = bytearray(f.read())
+    raw[0] = 0x00
+    open(p + ".bed", "wb").write(bytes(raw))
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.probe(p)
+    assert e.value.status == 3
+    # individual-major mode byte
+    raw[0] = 0x6C
+    raw[2] = 0x00
+    open(p + ".bed", "wb").write(bytes(raw))
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.probe(p)
+    assert e.value.status == 3 and "individual-major" in e.value.message
+    # truncated .bed
+    raw[2] = 0x01
+    open(p + ".bed", "wb").write(bytes(raw[:-10]))
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.probe(p)
+    assert e.value.status == 3
+    # .fam whose last line has no newline: not counted (distpca.cpp:137-147)
+    open(p + ".bed", "wb").write(bytes(raw))
+    with open(prefix + ".fam") as f:
+        fam = f.read()
+    open(p + ".fam", "w").write(fam + "EXTRA\tX\t0\t0\t0\t-9")
+    assert dpca.probe(p) == (203, 2500)
+
+
+def _fake_result(dpca, n_ind, sigma, u):
+    r = dpca.Result()
+    r.n_ind, r.nsv = n_ind, len(sigma)
+    r.sigma = sigma.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    r.u = u.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    return r
+
+
+def test_writers_match_reference_format(dpca, golden, tmp_path):
+    # feed the reference's own values through our writer: the files must be byte-identical
+    prefix = os.path.join(GOLDEN, "small")
+    sigma = np.ascontiguousarray(golden["run_small_ooc_sigma"])
+    u = np.ascontiguousarray(golden["run_small_ooc_u"])
+    c = dpca.config(prefix=str(tmp_path / "r"))
+    r = _fake_result(dpca, 203, sigma, u)
+    assert dpca.lib().dpca_write_outputs(ctypes.byref(c), prefix.encode(), ctypes.byref(r)) == 0
+    for suffix in ("singularValues", "leftSingularVectors"):
+        mine = open(str(tmp_path / f"r_{suffix}.txt")).read().splitlines()
+        ref = open(os.path.join(GOLDEN, f"small_ooc_ref_{suffix}.txt")).read().splitlines()
+        assert mine[: len(ref)] == ref
+
+
+def test_statistics_block_lines(dpca, tmp_path):
+    script = (
+        "import ctypes, sys; sys.path.insert(0, %r); import distpca_gb300 as D;"
+        "c = D.config(); r = D.Result(); r.n_ind = 942; r.n_snp = 133594; r.nsv = 20; r.nrhs = 40;"
+        "r.rows_fetched = 100; r.total_its = 11; r.time_load_matrix = 1.5;"
+        "D.lib().dpca_print_statistics(ctypes.byref(c), ctypes.byref(r))" % ROOT)
+    out = subprocess.run(["python", "-c", script], capture_output=True, text=True, check=True).stdout
+    assert "Total number of times which the data matrix was fetched from the memory: 22" in out
+    assert "Total number of matrix rows: 942" in out
+    assert "Time to load the data matrix: 1.5000000000000" in out
+    assert out.count("Total wall-clock time elapsed:") == 2
+
+
+def test_no_device_is_a_loud_error(dpca):
+    from conftest import gpu_available
+
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.Handle(100, 100, 4)
+    assert e.value.status == 4 and "no CPU fallback" in e.value.message
+    prefix, n_ind, n_snp, packed = fileset("tiny")
+    with pytest.raises(dpca.DpcaError):
+        dpca.decode_counts(packed, n_ind)
