@@ -220,7 +220,8 @@ def dpca_arm(a, ranks: Ranks) -> None:
 
     dev = ranks.local
     torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the library launches on it and the events below time it
+    stream = torch.cuda.Stream(device=dev)
     c = synth.config_cohort("incore50k", n_snp=a.n_snp, n_ind=a.n_ind)
     prec = D.PREC_MIXED if a.precision == "mixed" else D.PREC_FP64
     h = D.Handle(a.n_ind, a.n_snp, a.nrhs, precision=prec, device=dev, stream=stream.cuda_stream)
@@ -301,17 +302,18 @@ def fp64_comparison(a, hv, mixed_per_gpu: float) -> dict:
     import distpca_gb300 as D
 
     S = min(a.fp64_snps, a.n_snp)
-    with D.Handle(a.n_ind, S, a.nrhs, precision=D.PREC_FP64, stream=torch.cuda.current_stream().cuda_stream) as h:
+    stream = torch.cuda.Stream()
+    with D.Handle(a.n_ind, S, a.nrhs, precision=D.PREC_FP64, stream=stream.cuda_stream) as h:
         h.upload_ptr(hv.ctypes.data, hv.shape[1])
         h.set_omega(D.start_block(a.n_ind, a.nrhs))
         h.pass_()
         h.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
+        e0.record(stream)
         for _ in range(2):
             h.pass_()
-        e1.record()
+        e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / 2
     v = a.n_ind * S / (ms / 1e3)

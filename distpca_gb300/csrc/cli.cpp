@@ -9,10 +9,13 @@
 // does before exiting).
 #include <cmath>
 #include <cstdio>
+#include <fstream>
+#include <sstream>
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "dpca.h"
@@ -23,6 +26,22 @@ static std::string stamp() {
     std::string str(s);
     if (!str.empty() && str.back() == '\n') str.pop_back();
     return "[" + str + "] ";
+}
+
+// IIDs (.fam column 2) of the newline-terminated lines, as GetFamInfo collects them.
+static std::vector<std::string> read_iids(const std::string &fam) {
+    std::vector<std::string> ids;
+    std::ifstream in(fam.c_str());
+    while (in) {
+        std::string line;
+        std::getline(in, line);
+        if (in.eof()) break;
+        std::stringstream ss(line);
+        std::string a, b;
+        ss >> a >> b;
+        ids.push_back(b);
+    }
+    return ids;
 }
 
 static int fail(dpca_status st) {
@@ -76,8 +95,19 @@ int main(int argc, char **argv) {
         if (st != DPCA_OK) return fail(st);
     }
     if (cfg.verbose > 1) {
+        // distpca.cpp:409-439
         printf("\nApproximate eigenvalues:\n");
         for (int j = 0; j < res.nsv; ++j) printf("λ_%d = %.13f\n", j, sigma[j] * sigma[j]);
+        printf("\nFirst 5 individuals' eigenvectors:\n\n");
+        printf("%-20s", "FID");
+        for (int j = 0; j < res.nsv; ++j) printf("%-15s", ("PC" + std::to_string(j)).c_str());
+        printf("\n%s\n", std::string(20 + 15 * res.nsv, '-').c_str());
+        std::vector<std::string> iids = read_iids(std::string(bfile) + ".fam");
+        for (int i = 0; i < std::min(5, M); ++i) {
+            printf("%-20s", i < (int)iids.size() ? iids[i].c_str() : "");
+            for (int j = 0; j < res.nsv; ++j) printf("%-15.6f", u[(size_t)i * res.nsv + j]);
+            printf("\n");
+        }
     }
     if (cfg.verbose > 0) dpca_print_statistics(&cfg, &res);
     return 0;

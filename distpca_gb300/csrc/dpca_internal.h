@@ -83,7 +83,6 @@ struct Handle {
     double *avg = nullptr, *sd = nullptr;
     double *lut = nullptr;      // [n_snp][4] standardized value per raw code (times 1/sqrt(n_snp))
     double *coef = nullptr;     // [n_snp][2] mixed path: X = b*g + a*nonmissing -> {b, a}
-    double *rowbound = nullptr; // [n_snp] mixed path: max(|b|,|a|) * ||X_s||_2
     bool stats_ready = false;
 
     // dense FP64 state, n_ind x k row-major unless noted
@@ -134,7 +133,6 @@ dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol,
 // mixed-precision pass (k_mixed.cu)
 dpca_status mixed_prepare(Handle *h);
 dpca_status mixed_release(Handle *h);
-dpca_status mixed_after_stats(Handle *h);  // per-SNP bound reduction used to scale b.Y, a.Y
 dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out_or_null);
 dpca_status launch_mixed_xty(Handle *h, double *z);
 

@@ -98,7 +98,7 @@ static dpca_status dalloc(T **p, size_t elems) {
 
 static void free_all(Handle *h) {
     if (h->mx) mixed_release(h);
-    void *ptrs[] = {h->P, h->PT, h->counts, h->avg, h->sd, h->lut, h->coef, h->rowbound, h->omega, h->z, h->q,
+    void *ptrs[] = {h->P, h->PT, h->counts, h->avg, h->sd, h->lut, h->coef, h->omega, h->z, h->q,
                     h->old, h->work, h->y, h->partial, h->small, h->red, h->dflag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -158,7 +158,6 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
     DPCA_TRY(dalloc(&h->sd, (size_t)n_snp));
     DPCA_TRY(dalloc(&h->lut, 4 * (size_t)n_snp));
     DPCA_TRY(dalloc(&h->coef, 2 * (size_t)n_snp));
-    DPCA_TRY(dalloc(&h->rowbound, (size_t)n_snp));
     DPCA_TRY(dalloc(&h->omega, nk));
     DPCA_TRY(dalloc(&h->z, nk));
     DPCA_TRY(dalloc(&h->q, nk));
@@ -195,7 +194,6 @@ static dpca_status after_data(Handle *h) {
     DPCA_TRY(launch_snp_stats(h));
     if (h->precision == DPCA_PREC_MIXED) {
         DPCA_TRY(launch_transpose_packed(h));
-        DPCA_TRY(mixed_after_stats(h));
     }
     h->stats_ready = true;
     return DPCA_OK;

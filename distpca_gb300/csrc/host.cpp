@@ -128,37 +128,38 @@ static dpca_status run_common(const dpca_config *cfg_in, const char *bfile, cons
     cfg.bsize = rows;
     res->rows_fetched = rows;
     double t0 = wall_now();
+    dpca_handle *hh = nullptr;
+    DPCA_TRY(dpca_create(&hh, n_ind, n_snp, cfg.nrhs, cfg.precision, cfg.device, nullptr));
     std::vector<uint8_t> filebuf;
     uint8_t *pinned = nullptr;
     const uint8_t *src = packed_host;
     int64_t stride = row_stride;
     int64_t np = (n_ind + 3) / 4;
+    dpca_status st = DPCA_OK;
     if (!src) {
-        // read the whole .bed payload into pinned memory
+        // the whole .bed payload, in pinned memory when the host allows it
         std::string bed = std::string(bfile) + ".bed";
         int fd = open(bed.c_str(), O_RDONLY);
         if (fd < 0) {
+            dpca_destroy(hh);
             set_error("[Data::read_bed] Error reading file %s", bed.c_str());
             return DPCA_ERR_IO;
         }
         size_t bytes = (size_t)np * n_snp;
-        if (cudaMallocHost((void **)&pinned, std::max<size_t>(bytes, 1)) != cudaSuccess) {
+        uint8_t *buf = nullptr;
+        if (cudaMallocHost((void **)&pinned, std::max<size_t>(bytes, 1)) == cudaSuccess) {
+            buf = pinned;
+        } else {
             cudaGetLastError();
-            close(fd);
-            set_error("cannot pin %zu bytes of host memory for %s", bytes, bed.c_str());
-            return DPCA_ERR_NOMEM;
+            pinned = nullptr;
+            filebuf.resize(bytes);
+            buf = filebuf.data();
         }
-        dpca_status st = pread_all(fd, pinned, bytes, 3, bed.c_str());
+        st = pread_all(fd, buf, bytes, 3, bed.c_str());
         close(fd);
-        if (st != DPCA_OK) {
-            cudaFreeHost(pinned);
-            return st;
-        }
-        src = pinned;
+        src = buf;
         stride = np;
     }
-    dpca_handle *hh = nullptr;
-    dpca_status st = dpca_create(&hh, n_ind, n_snp, cfg.nrhs, cfg.precision, cfg.device, nullptr);
     if (st == DPCA_OK) st = dpca_upload(hh, src, stride);
     if (st == DPCA_OK) st = dpca_synchronize(hh);
     double t1 = wall_now();

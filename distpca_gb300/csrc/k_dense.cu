@@ -219,7 +219,7 @@ dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, doubl
     size_t smem = (size_t)2 * 32 * k * sizeof(double);
     {
         ScopedLaunch t(&h->clock, h->stream, "atb");
-        if (smem > 48 * 1024) cudaFuncSetAttribute(atb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(atb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         atb_kernel<<<nparts, 256, smem, h->stream>>>(a, b, n, k, rpb, h->red);
         DPCA_CUDA(cudaGetLastError());
     }
@@ -331,8 +331,7 @@ dpca_status launch_eig_desc(Handle *h) {
     int k = h->k;
     SmallLayout L{k};
     size_t smem = (size_t)k * (k + 1) * sizeof(double) + 2 * 64 * sizeof(double) + (k + 2) * sizeof(int);
-    if (smem > 48 * 1024)
-        DPCA_CUDA(cudaFuncSetAttribute(jacobi_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DPCA_CUDA(cudaFuncSetAttribute(jacobi_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     jacobi_eig_kernel<<<1, 512, smem, h->stream>>>(h->small + L.B(), k, h->small + L.W(), h->small + L.w(), h->red,
                                                    60);
     DPCA_CUDA(cudaGetLastError());
@@ -360,8 +359,7 @@ dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
     ScopedLaunch t(&h->clock, h->stream, "apply_w");
     int k = h->k;
     size_t smem = (size_t)k * k * sizeof(double);
-    if (smem > 48 * 1024)
-        DPCA_CUDA(cudaFuncSetAttribute(apply_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DPCA_CUDA(cudaFuncSetAttribute(apply_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int64_t total = (int64_t)h->n_ind * k;
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
     apply_w_kernel<<<grid, 256, smem, h->stream>>>(q, h->small + SmallLayout{k}.W(), h->n_ind, k, out);

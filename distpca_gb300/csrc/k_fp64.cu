@@ -139,8 +139,8 @@ __global__ void reduce_splits_kernel(const double *__restrict__ partial, int64_t
 template <int MAXC>
 static void xw_launch(Handle *h, const double *omega, double *y) {
     size_t smem = (size_t)64 * h->k * sizeof(double);
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(fp64_xw_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // opt in above the default 48 KB (static shared memory counts against it as well)
+    cudaFuncSetAttribute(fp64_xw_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     fp64_xw_kernel<MAXC><<<ceil_div(h->n_snp, 64), 256, smem, h->stream>>>(h->P, h->pitch, h->lut, h->n_ind,
                                                                             h->n_snp, h->k, omega, y);
 }
@@ -169,6 +169,7 @@ static int xty_splits(const Handle *h) {
 template <int MAXC>
 static void xty_launch(Handle *h, const double *y, int splits, int sps) {
     size_t smem = (size_t)32 * h->k * sizeof(double);
+    cudaFuncSetAttribute(fp64_xty_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid(ceil_div(h->n_ind, 128), splits);
     fp64_xty_kernel<MAXC><<<grid, 512, smem, h->stream>>>(h->P, h->pitch, h->lut, h->n_ind, h->n_snp, h->k, y,
                                                            h->partial, sps);

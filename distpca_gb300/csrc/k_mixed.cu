@@ -6,20 +6,35 @@
 // so the two products of the pass (methods.cpp:853-854, 862-863) become
 //     Y  = X Omega  = diag(b) (G' Omega) + diag(a) (M Omega)                      (gemm<kXW>)
 //     Z  = X^T Y    = G'^T (b.Y) + M^T (a.Y)                                      (gemm<kXTY>)
-// G' and M are exact in FP16.  The dense operands (Omega; b.Y and a.Y) are scaled per column by a
-// power of two and split into hi + lo FP16 halves (22 significant bits), laid side by side along
-// the MMA's N dimension ([hi | lo], N = 2*round_up(k, 8)), and accumulated in FP32 in TMEM.
-// The per-SNP coefficients, the hi+lo recombination and the scale removal run in FP64 in the
-// epilogues.
 //
-// Kernel structure (one CTA per 128-row output tile, 192 threads):
-//   warp 0      TMA producer: packed 2-bit tiles [128 rows x 128 B] (SWIZZLE_128B) and FP16
-//               operand tiles [N rows x 64 elements] (SWIZZLE_128B).
-//   warp 1      TMEM allocation and the single MMA-issuing thread
-//               (tcgen05.mma.kind::f16, A from tensor memory, B from shared memory).
-//   warps 2..5  decode: one thread per tile row turns 16 packed bytes (64 genotypes) into
-//               32+32 FP16 pairs with byte-permute table lookups and stores them into TMEM
-//               (tcgen05.st); afterwards the same warps run the epilogue (tcgen05.ld).
+// Exactness.  The tensor core adds into its FP32 accumulator with truncation (round toward
+// zero), which biases long sums.  So every product and partial sum is made an integer below 2^24,
+// where truncation cannot lose a bit:
+//   - G' and M are exact small integers in FP16;
+//   - each dense operand column (Omega; b.Y and a.Y) is scaled by the power of two that puts its
+//     largest magnitude just under 2^23 and rounded to the nearest integer v (24-bit fixed
+//     point, an unbiased quantisation), stored as two integer FP16 slices v = 4096 h + l with
+//     h, l in [-2048, 2048] (FP16 holds every such integer exactly), laid side by side along the
+//     MMA's N dimension ([h | l], N = 2*round_up(k, 8));
+//   - a TMEM accumulator sums at most kChunkXW (resp. kChunkXTY) K-blocks, which bounds every
+//     partial sum below 2^24, then four accumulator warps fold it into FP64 (in shared memory)
+//     while the tensor core fills the other of two accumulator sets.
+// The per-SNP coefficients, the slice recombination and the scale removal run in FP64.  The
+// X Omega epilogue writes Y (FP32, transposed) and the exact column maxima of |b.Y|, |a.Y|, from
+// which a split kernel quantises the X^T Y operand.
+//
+// CTA structure (one CTA per 128-row output tile and K split, 480 threads, 1 CTA per SM):
+//   warp 0       TMA producer: packed 2-bit tiles [128 rows x 128 B] and FP16 slice tiles
+//                [N rows x 64 elements], both 128-byte swizzled.
+//   warps 1, 14  TMEM allocation (warp 1) and the two MMA-issuing threads
+//                (tcgen05.mma.kind::f16, A from tensor memory, B from shared memory): warp 1
+//                issues the G' products, warp 14 the M products, each into its own accumulator,
+//                because one thread cannot issue N=80 MMAs as fast as the tensor core runs them.
+//   warps 2..9   decode, two groups of four warps on alternating K-blocks: one thread per tile
+//                row turns 16 packed bytes (64 genotypes) into 32+32 FP16 pairs with
+//                byte-permute table lookups and stores them into TMEM (tcgen05.st).
+//   warps 10..13 accumulate: drain finished TMEM accumulator chunks (tcgen05.ld) into FP64 and
+//                write the outputs.
 // Pipelines are mbarrier rings; every wait is bounded (tc.cuh) and reports through h->dflag.
 #include <cuda_fp16.h>
 
@@ -34,11 +49,21 @@ namespace dpca {
 
 constexpr int kXW = 1;   // Y = X Omega (rows = SNPs, K = individuals)
 constexpr int kXTY = 2;  // Z = X^T Y   (rows = individuals, K = SNPs)
-constexpr int kThreads = 192;
+constexpr int kWarps = 15;
+constexpr int kIssuerWarpM = 14;
+constexpr int kThreads = 32 * kWarps;
+constexpr int kDecodeGroups = 2;
 constexpr int kPStages = 3;
-constexpr int kPStageBytes = 128 * 128;  // 128 rows x 128 B = 512 K-elements
+constexpr int kPStageBytes = 128 * 128;  // 128 rows x 128 B = 512 K-elements = 8 K-blocks
 constexpr int kTmemCols = 512;
 constexpr int kSmemFloor = 120 * 1024;   // keeps one CTA per SM (the CTA owns all of TMEM)
+// K-blocks per exact accumulation chunk.  One K step (16 products) adds at most 16*2*2048 = 2^16
+// to an X Omega accumulator and 16*(2+1)*2048 = 1.5*2^16 to an X^T Y accumulator; chunks keep
+// |partial sum| + one step's products below 2^24 (48*4 = 192 and 32*4 = 128 steps), so every
+// intermediate value is an integer the FP32 accumulator holds exactly.
+constexpr int kChunkXW = 48;
+constexpr int kChunkXTY = 32;
+constexpr int kMaxMixedNrhs = 48;        // two accumulator sets of 2 x N columns fit TMEM
 
 struct GemmArgs {
     int rows;          // valid output rows
@@ -48,8 +73,9 @@ struct GemmArgs {
     int sa, sb;        // A stages (TMEM), B stages (SMEM)
     const double *coef;     // kXW: [rows][2] {b, a}
     const double *scales;   // [4][k]: omega scale, its inverse, b/aY scale, its inverse
-    __half *bop;            // kXW: [2N][bop_ld]
-    int64_t bop_ld;
+    float *yt;              // kXW: Y transposed, [k][yt_ld] (FP32)
+    int64_t yt_ld;
+    unsigned int *colmax;   // kXW: per column, bits of max(|b.Y|, |a.Y|) (non-negative float)
     double *y_out;          // kXW: optional FP64 Y [rows][k]
     double *partial;        // kXTY: [splits][rows][k]
     int *err;
@@ -59,11 +85,12 @@ struct MixedState {
     int kp = 0, N = 0;
     __half *omega_s = nullptr;  // [N][n_ind_pad]
     __half *bop = nullptr;      // [2N][n_snp_pad]
+    float *yt = nullptr;        // [k][n_snp_pad]
+    unsigned int *colmax = nullptr;  // [k]
     double *scales = nullptr;   // [4][k]
-    double *rmax = nullptr;     // [1]
     double *partial = nullptr;  // [splits][n_ind][k]
     int splits = 1, kb_per_split = 8;
-    int sb1 = 2, sb2 = 2;
+    int sb1 = 2, sb2 = 2, sa1 = 2, sa2 = 2;
     size_t smem1 = 0, smem2 = 0;
     CUtensorMap map_p, map_pt, map_om, map_bop;
 };
@@ -88,9 +115,16 @@ __device__ __forceinline__ void decode64(uint4 v, uint32_t (&G)[32], uint32_t (&
         }
 }
 
-__device__ __forceinline__ void split_half(double v, __half &hi, __half &lo) {
-    hi = __double2half(v);
-    lo = __double2half(v - (double)__half2float(hi));
+// v (already scaled, |v| < 2^23) -> nearest integer n = 4096 h + l, h and l in [-2048, 2048].
+__device__ __forceinline__ void fixed_slices(double v, __half &hi, __half &lo) {
+    const double n = rint(v);
+    const double h = rint(n * (1.0 / 4096.0));
+    hi = __double2half(h);               // exact: |h| <= 2048
+    lo = __double2half(n - 4096.0 * h);  // exact: |l| <= 2048
+}
+
+__device__ __forceinline__ double slices_value(uint32_t hbits, uint32_t lbits) {
+    return 4096.0 * (double)__uint_as_float(hbits) + (double)__uint_as_float(lbits);
 }
 
 template <int MODE>
@@ -100,37 +134,43 @@ __global__ void __launch_bounds__(kThreads, 1)
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int N = args.N, kp = args.kp, SA = args.sa, SB = args.sb;
+    constexpr int kChunk = MODE == kXW ? kChunkXW : kChunkXTY;
     const int bstage = (MODE == kXW ? 1 : 2) * N * 128;
     uint8_t *sP = smem;
     uint8_t *sB = smem + kPStages * kPStageBytes;
-    uint64_t *bars = (uint64_t *)(sB + (size_t)SB * bstage);
+    double *acc64 = (double *)(sB + (size_t)SB * bstage);  // [kp][128] FP64 accumulators
+    uint64_t *bars = (uint64_t *)(acc64 + (size_t)kp * 128);
     uint64_t *pk_full = bars, *pk_empty = bars + kPStages;
     uint64_t *b_full = pk_empty + kPStages, *b_empty = b_full + SB;
     uint64_t *a_full = b_empty + SB, *a_empty = a_full + SA;
-    uint64_t *acc_full = a_empty + SA;
-    uint32_t *tmem_slot = (uint32_t *)(acc_full + 1);
+    uint64_t *acc_full = a_empty + SA, *acc_empty = acc_full + 2;
+    uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x, split = blockIdx.y;
     const int kb0 = split * args.kb_per_split;
     const int nkb = min(args.nkb_total, kb0 + args.kb_per_split) - kb0;
     const int npg = (nkb + 7) >> 3;
+    const int nchunks = (nkb + kChunk - 1) / kChunk;
     int *err = args.err;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kPStages; ++s) {
             tc::mbar_init(&pk_full[s], 1);
-            tc::mbar_init(&pk_empty[s], 128);
+            tc::mbar_init(&pk_empty[s], 128 * kDecodeGroups);
         }
         for (int s = 0; s < SB; ++s) {
             tc::mbar_init(&b_full[s], 1);
-            tc::mbar_init(&b_empty[s], 1);
+            tc::mbar_init(&b_empty[s], 2);  // one commit per MMA issuer
         }
         for (int s = 0; s < SA; ++s) {
             tc::mbar_init(&a_full[s], 128);
-            tc::mbar_init(&a_empty[s], 1);
+            tc::mbar_init(&a_empty[s], 2);
         }
-        tc::mbar_init(acc_full, 1);
+        for (int s = 0; s < 2; ++s) {
+            tc::mbar_init(&acc_full[s], 2);
+            tc::mbar_init(&acc_empty[s], 128);
+        }
         tc::fence_mbar_init();
         tc::tma_prefetch(&map_a);
         tc::tma_prefetch(&map_b);
@@ -143,8 +183,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = *tmem_slot;
-    // accumulators first; A stages (32 columns per variant) start on a 32-column boundary
-    const int a_base = ((MODE == kXW ? 2 : 1) * N + 31) & ~31;
+    // TMEM columns: accumulator set s at [s * set_cols, (s+1) * set_cols) -- the G' products'
+    // [h | l] block, then the M products' -- then the A stages (32 columns per variant) from a
+    // 32-column boundary.
+    const int set_cols = 2 * N;
+    const int a_base = (2 * set_cols + 31) & ~31;
     auto a_col = [&](int stage, int variant) -> uint32_t { return (uint32_t)(a_base + 64 * stage + 32 * variant); };
 
     if (warp == 0) {
@@ -154,7 +197,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             bool ok = true;
             for (int g = 0; g < npg && ok; ++g) {
                 const int sp = g % kPStages;
-                ok = tc::mbar_wait(&pk_empty[sp], ((g / kPStages) & 1) ^ 1, err, 11);
+                ok = tc::mbar_wait(&pk_empty[sp], ((g / kPStages) & 1) ^ 1, err, 11, true);
                 if (!ok) break;
                 tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
                 tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (kb0 + 8 * g) * 16, tile * 128);
@@ -162,7 +205,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int jn = min(8, nkb - 8 * g);
                 for (int j = 0; j < jn; ++j) {
                     const int kb = 8 * g + j, sb = kb % SB;
-                    ok = tc::mbar_wait(&b_empty[sb], ((kb / SB) & 1) ^ 1, err, 12);
+                    ok = tc::mbar_wait(&b_empty[sb], ((kb / SB) & 1) ^ 1, err, 12, true);
                     if (!ok) break;
                     tc::mbar_arrive_expect_tx(&b_full[sb], bstage);
                     uint8_t *dst = sB + (size_t)sb * bstage;
@@ -173,49 +216,50 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             // drain: every issued copy must land before the CTA may exit
             for (int g = max(0, issued_p - kPStages); g < issued_p; ++g)
-                tc::mbar_wait(&pk_full[g % kPStages], (g / kPStages) & 1, err, 13);
+                tc::mbar_wait(&pk_full[g % kPStages], (g / kPStages) & 1, err, 13, true);
             for (int kb = max(0, issued_b - SB); kb < issued_b; ++kb)
-                tc::mbar_wait(&b_full[kb % SB], (kb / SB) & 1, err, 14);
+                tc::mbar_wait(&b_full[kb % SB], (kb / SB) & 1, err, 14, true);
         }
-    } else if (warp == 1) {
-        // ---------------------------------------------------------- MMA issuer
+    } else if (warp == 1 || warp == kIssuerWarpM) {
+        // ---------------------------------------------------------- MMA issuers
         if (lane == 0) {
+            const int v = warp == 1 ? 0 : 1;  // 0: G' products, 1: M products
             const uint32_t idesc = tc::idesc_f16_f32(128, N);
-            const uint32_t sB_addr = tc::smem_u32(sB);
+            // descriptor of B stage 0 (for X^T Y the M products use the stage's second half);
+            // a stage is bstage bytes further, a K step 32 bytes = 2 descriptor units
+            const uint64_t bdesc0 =
+                tc::desc_kmajor_sw128(tc::smem_u32(sB) + (MODE == kXTY ? (uint32_t)(v * N * 128) : 0u));
+            const uint32_t a_v = tbase + a_col(0, v);
             for (int kb = 0; kb < nkb; ++kb) {
+                const int chunk = kb / kChunk, set = chunk & 1;
+                const bool first = (kb % kChunk) == 0;
+                if (first && chunk >= 2 && !tc::mbar_wait(&acc_empty[set], ((chunk >> 1) - 1) & 1, err, 23)) break;
                 const int sb = kb % SB, sa = kb % SA;
                 if (!tc::mbar_wait(&b_full[sb], (kb / SB) & 1, err, 21)) break;
                 if (!tc::mbar_wait(&a_full[sa], (kb / SA) & 1, err, 22)) break;
                 tc::fence_after_sync();
-                const uint32_t bst = sB_addr + (uint32_t)(sb * bstage);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    const uint64_t bdesc = tc::desc_kmajor_sw128(bst + 32 * kk);
-                    const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
-                    const uint32_t ag = tbase + a_col(sa, 0) + 8 * kk, am = tbase + a_col(sa, 1) + 8 * kk;
-                    if (MODE == kXW) {
-                        tc::mma_ts_f16(tbase, ag, bdesc, idesc, acc);
-                        tc::mma_ts_f16(tbase + N, am, bdesc, idesc, acc);
-                    } else {
-                        tc::mma_ts_f16(tbase, ag, bdesc, idesc, acc);
-                        tc::mma_ts_f16(tbase, am, tc::desc_kmajor_sw128(bst + N * 128 + 32 * kk), idesc, 1u);
-                    }
-                }
+                const uint64_t bd = bdesc0 + (uint64_t)((sb * bstage) >> 4);
+                const uint32_t d = tbase + (uint32_t)(set * set_cols + v * N);
+                const uint32_t a = a_v + (uint32_t)(64 * sa);
+                tc::mma_ts_f16(d, a, bd, idesc, first ? 0u : 1u);
+                tc::mma_ts_f16(d, a + 8, bd + 2, idesc, 1u);
+                tc::mma_ts_f16(d, a + 16, bd + 4, idesc, 1u);
+                tc::mma_ts_f16(d, a + 24, bd + 6, idesc, 1u);
                 tc::mma_commit(&b_empty[sb]);
                 tc::mma_commit(&a_empty[sa]);
+                if ((kb % kChunk) == kChunk - 1 || kb == nkb - 1) tc::mma_commit(&acc_full[set]);
             }
-            tc::mma_commit(acc_full);
         }
-    } else {
-        // ---------------------------------------------------------- decode (warps 2..5)
+    } else if (warp >= 2 && warp < 2 + 4 * kDecodeGroups) {
+        // ---------------------------------------------------------- decode (warps 2..9)
+        const int grp = (warp - 2) >> 2;
         const int q = warp & 3;
         const int r = 32 * q + lane;
         const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
         uint32_t G[32], M[32];
-        for (int kb = 0; kb < nkb; ++kb) {
+        for (int kb = grp; kb < nkb; kb += kDecodeGroups) {
             const int g = kb >> 3, j = kb & 7, sp = g % kPStages, sa = kb % SA;
-            bool ok = true;
-            if (j == 0) ok = tc::mbar_wait(&pk_full[sp], (g / kPStages) & 1, err, 31);
+            bool ok = tc::mbar_wait(&pk_full[sp], (g / kPStages) & 1, err, 31);
             ok = ok && tc::mbar_wait(&a_empty[sa], ((kb / SA) & 1) ^ 1, err, 32);
             if (!__all_sync(0xffffffffu, ok)) break;  // TMEM stores below are warp-collective
             const uint4 v = *reinterpret_cast<const uint4 *>(sP + sp * kPStageBytes + r * 128 + ((j ^ (r & 7)) << 4));
@@ -225,61 +269,73 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::tmem_wait_st();
             tc::fence_before_sync();
             tc::mbar_arrive(&a_full[sa]);
-            if (j == 7 || kb == nkb - 1) tc::mbar_arrive(&pk_empty[sp]);
+            // last K-block of this group inside the packed stage: release the stage
+            if (kb + kDecodeGroups > min(8 * g + 7, nkb - 1)) tc::mbar_arrive(&pk_empty[sp]);
         }
-        // ---------------------------------------------------------- epilogue
-        const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full, 0, err, 41));
-        tc::fence_after_sync();
+    } else if (warp < 14) {
+        // ---------------------------------------------------------- accumulate (warps 10..13)
+        const int q = warp & 3;
+        const int r = 32 * q + lane;
+        const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
         const int row = tile * 128 + r;
-        const bool valid = ok && row < args.rows;
         const int k = args.k;
+        double b = 0.0, a = 0.0;
+        if (MODE == kXW && row < args.rows) {
+            b = args.coef[2 * (size_t)row];
+            a = args.coef[2 * (size_t)row + 1];
+        }
+        for (int c = 0; c < kp; ++c) acc64[c * 128 + r] = 0.0;
+        bool ok = true;
+        for (int chunk = 0; chunk < nchunks; ++chunk) {
+            const int set = chunk & 1;
+            ok = __all_sync(0xffffffffu, ok && tc::mbar_wait(&acc_full[set], (chunk >> 1) & 1, err, 41, true));
+            if (!ok) break;
+            tc::fence_after_sync();
+            const uint32_t cb = lane_base + (uint32_t)(set * set_cols);
+            for (int c0 = 0; c0 < kp; c0 += 8) {
+                if (MODE == kXW) {
+                    uint32_t gh[8], gl[8], mh[8], ml[8];
+                    tc::tmem_ld_x8(cb + c0, gh);
+                    tc::tmem_ld_x8(cb + kp + c0, gl);
+                    tc::tmem_ld_x8(cb + N + c0, mh);
+                    tc::tmem_ld_x8(cb + N + kp + c0, ml);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int jj = 0; jj < 8; ++jj)
+                        acc64[(c0 + jj) * 128 + r] += b * slices_value(gh[jj], gl[jj]) + a * slices_value(mh[jj], ml[jj]);
+                } else {
+                    uint32_t gh[8], gl[8], mh[8], ml[8];
+                    tc::tmem_ld_x8(cb + c0, gh);
+                    tc::tmem_ld_x8(cb + kp + c0, gl);
+                    tc::tmem_ld_x8(cb + N + c0, mh);
+                    tc::tmem_ld_x8(cb + N + kp + c0, ml);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int jj = 0; jj < 8; ++jj)
+                        acc64[(c0 + jj) * 128 + r] += slices_value(gh[jj], gl[jj]) + slices_value(mh[jj], ml[jj]);
+                }
+            }
+            tc::fence_before_sync();
+            tc::mbar_arrive(&acc_empty[set]);
+        }
+        const bool valid = ok && row < args.rows;
         const double *sc = args.scales;
         if (MODE == kXW) {
-            const double b = valid ? args.coef[2 * (size_t)row] : 0.0;
-            const double a = valid ? args.coef[2 * (size_t)row + 1] : 0.0;
-            for (int c0 = 0; c0 < kp; c0 += 8) {
-                uint32_t gh[8], gl[8], mh[8], ml[8];
-                tc::tmem_ld_x8(lane_base + c0, gh);
-                tc::tmem_ld_x8(lane_base + kp + c0, gl);
-                tc::tmem_ld_x8(lane_base + N + c0, mh);
-                tc::tmem_ld_x8(lane_base + N + kp + c0, ml);
-                tc::tmem_wait_ld();
-                if (!valid) continue;
-#pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                    const int c = c0 + jj;
-                    if (c >= k) break;
-                    const double dg = (double)__uint_as_float(gh[jj]) + (double)__uint_as_float(gl[jj]);
-                    const double dm = (double)__uint_as_float(mh[jj]) + (double)__uint_as_float(ml[jj]);
-                    const double y = (b * dg + a * dm) * sc[k + c];
+            for (int c = 0; c < k; ++c) {
+                float mag = 0.f;
+                if (valid) {
+                    const double y = acc64[c * 128 + r] * sc[k + c];
                     if (args.y_out) args.y_out[(size_t)row * k + c] = y;
-                    const double s2 = sc[2 * k + c];
-                    __half h1, l1, h2, l2;
-                    split_half(b * y * s2, h1, l1);
-                    split_half(a * y * s2, h2, l2);
-                    __half *bo = args.bop + row;
-                    const int64_t ld = args.bop_ld;
-                    bo[(int64_t)c * ld] = h1;
-                    bo[(int64_t)(kp + c) * ld] = l1;
-                    bo[(int64_t)(N + c) * ld] = h2;
-                    bo[(int64_t)(N + kp + c) * ld] = l2;
+                    args.yt[(int64_t)c * args.yt_ld + row] = (float)y;
+                    mag = (float)(fmax(fabs(b), fabs(a)) * fabs(y));
                 }
-            }
-        } else {
-            double *out = args.partial + ((size_t)split * args.rows + row) * k;
-            for (int c0 = 0; c0 < kp; c0 += 8) {
-                uint32_t hi[8], lo[8];
-                tc::tmem_ld_x8(lane_base + c0, hi);
-                tc::tmem_ld_x8(lane_base + kp + c0, lo);
-                tc::tmem_wait_ld();
-                if (!valid) continue;
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                    const int c = c0 + jj;
-                    if (c >= k) break;
-                    out[c] = ((double)__uint_as_float(hi[jj]) + (double)__uint_as_float(lo[jj])) * sc[3 * k + c];
-                }
+                for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
+                if (lane == 0 && mag > 0.f) atomicMax(args.colmax + c, __float_as_uint(mag));
             }
+        } else if (valid) {
+            double *out = args.partial + ((size_t)split * args.rows + row) * k;
+            for (int c = 0; c < k; ++c) out[c] = acc64[c * 128 + r] * sc[3 * k + c];
         }
     }
     tc::fence_before_sync();
@@ -289,58 +345,33 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // ------------------------------------------------------------------ operand preparation
-// max over SNPs of max(|a|,|b|) * ||X_s||_2 (single block, fixed order).
-__global__ void __launch_bounds__(1024) rowbound_max_kernel(const double *rb, int n, double *out) {
-    __shared__ double red[32];
-    double m = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, rb[i]);
-    m = warp_max(m);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        m = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-        m = warp_max(m);
-        if (threadIdx.x == 0) out[0] = m;
-    }
-}
-
 __device__ __forceinline__ double pow2_scale_below(double bound) {
-    // largest power of two s with bound * s < 2^15 (1 when bound is 0 or not finite)
+    // largest power of two s with bound * s < 2^23 (1 when bound is 0 or not finite)
     if (!(bound > 0.0) || !isfinite(bound)) return 1.0;
     int e;
     frexp(bound, &e);  // bound < 2^e
-    return ldexp(1.0, 15 - e);
+    return ldexp(1.0, 23 - e);
 }
 
-// Block per column c of Omega: scale factors for the hi/lo split of Omega and of b.Y, a.Y
-// (|b_s Y_sc|, |a_s Y_sc| <= max_s(max(|a_s|,|b_s|) ||X_s||) * ||Omega_c|| by Cauchy-Schwarz).
+// Block per column c of Omega: the power-of-two scale for its fixed-point slices.
 __global__ void __launch_bounds__(256) omega_scales_kernel(const double *__restrict__ om, int n, int k,
-                                                           const double *__restrict__ rmax,
                                                            double *__restrict__ scales) {
-    __shared__ double red[32];
     __shared__ double redm[32];
     const int c = blockIdx.x;
-    double mx = 0.0, ss = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double v = om[(size_t)i * k + c];
-        mx = fmax(mx, fabs(v));
-        ss += v * v;
-    }
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, fabs(om[(size_t)i * k + c]));
     mx = warp_max(mx);
     if ((threadIdx.x & 31) == 0) redm[threadIdx.x >> 5] = mx;
-    ss = block_sum(ss, red);
+    __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, redm[w]);
-        double so = pow2_scale_below(mx);
-        double sb = pow2_scale_below(rmax[0] * sqrt(ss) * (1.0 + 1e-3));
+        const double so = pow2_scale_below(mx);
         scales[c] = so;
         scales[k + c] = 1.0 / so;
-        scales[2 * k + c] = sb;
-        scales[3 * k + c] = 1.0 / sb;
     }
 }
 
-// omega_s[c][i] = hi, omega_s[kp + c][i] = lo of Omega[i][c] * scale_c; zero padding elsewhere.
+// omega_s[c][i] = h, omega_s[kp + c][i] = l of round(Omega[i][c] * scale_c); zero padding elsewhere.
 __global__ void __launch_bounds__(256) omega_split_kernel(const double *__restrict__ om, int n, int k, int kp,
                                                           int n_pad, const double *__restrict__ scales,
                                                           __half *__restrict__ out) {
@@ -348,9 +379,34 @@ __global__ void __launch_bounds__(256) omega_split_kernel(const double *__restri
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int c = (int)(e / n_pad), i = (int)(e - (int64_t)c * n_pad);
         __half hi = __float2half(0.f), lo = __float2half(0.f);
-        if (c < k && i < n) split_half(om[(size_t)i * k + c] * scales[c], hi, lo);
+        if (c < k && i < n) fixed_slices(om[(size_t)i * k + c] * scales[c], hi, lo);
         out[(int64_t)c * n_pad + i] = hi;
         out[(int64_t)(kp + c) * n_pad + i] = lo;
+    }
+}
+
+// Scale per column from the exact maxima, then quantise b.Y and a.Y into the X^T Y operand:
+// bop[c] = h(b.Y), bop[kp+c] = l(b.Y), bop[N+c] = h(a.Y), bop[N+kp+c] = l(a.Y).
+__global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict__ yt, int64_t ld, int n_snp, int k,
+                                                        int kp, int N, const double *__restrict__ coef,
+                                                        const unsigned int *__restrict__ colmax,
+                                                        double *__restrict__ scales, __half *__restrict__ bop) {
+    const int64_t total = (int64_t)k * n_snp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e / n_snp), s = (int)(e - (int64_t)c * n_snp);
+        const double sc = pow2_scale_below((double)__uint_as_float(colmax[c]) * 1.001);
+        if (s == 0) {
+            scales[2 * k + c] = sc;
+            scales[3 * k + c] = 1.0 / sc;
+        }
+        const double y = (double)yt[(int64_t)c * ld + s] * sc;
+        __half h1, l1, h2, l2;
+        fixed_slices(coef[2 * (size_t)s] * y, h1, l1);
+        fixed_slices(coef[2 * (size_t)s + 1] * y, h2, l2);
+        bop[(int64_t)c * ld + s] = h1;
+        bop[(int64_t)(kp + c) * ld + s] = l1;
+        bop[(int64_t)(N + c) * ld + s] = h2;
+        bop[(int64_t)(N + kp + c) * ld + s] = l2;
     }
 }
 
@@ -404,19 +460,20 @@ static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base
 
 static MixedState *mstate(Handle *h) { return (MixedState *)h->mx; }
 
-static size_t smem_bytes(int mode, int N, int sb, int sa) {
+static size_t smem_bytes(int mode, int N, int kp, int sb, int sa) {
     size_t b = 1024 + (size_t)kPStages * kPStageBytes + (size_t)sb * (mode == kXW ? 1 : 2) * N * 128 +
-               (size_t)(2 * kPStages + 2 * sb + 2 * sa + 1) * 8 + 16;
+               (size_t)kp * 128 * 8 + (size_t)(2 * kPStages + 2 * sb + 2 * sa + 4) * 8 + 16;
     return std::max<size_t>(b, kSmemFloor);
 }
 
-static int pick_sb(int mode, int N) {
-    const size_t budget = 200 * 1024 - (size_t)kPStages * kPStageBytes;
+static int pick_sb(int mode, int N, int kp) {
+    const size_t budget = 210 * 1024 - (size_t)kPStages * kPStageBytes - (size_t)kp * 128 * 8;
     int sb = (int)(budget / ((size_t)(mode == kXW ? 1 : 2) * N * 128));
     return std::max(2, std::min(8, sb));
 }
 
-static int pick_sa(int acc_cols) { return std::min(8, (kTmemCols - ((acc_cols + 31) & ~31)) / 64); }
+static int pick_sa(int set_cols) { return std::min(8, (kTmemCols - ((2 * set_cols + 31) & ~31)) / 64); }
+// both products keep one accumulator per MMA issuer: a set is 2 x N columns
 
 dpca_status mixed_prepare(Handle *h) {
     const int k = h->k;
@@ -425,17 +482,24 @@ dpca_status mixed_prepare(Handle *h) {
     h->mx = m;
     m->kp = (k + 7) / 8 * 8;
     m->N = 2 * m->kp;
-    if (m->N > 192) {
-        set_error("mixed precision supports nrhs <= 96 (got %d); use the FP64 path", k);
+    if (k > kMaxMixedNrhs) {
+        set_error("mixed precision supports nrhs <= %d (got %d); use the FP64 path", kMaxMixedNrhs, k);
         return DPCA_ERR_UNSUPPORTED;
     }
     const int N = m->N;
+    m->sa1 = pick_sa(2 * N);
+    m->sa2 = pick_sa(2 * N);
+    if (m->sa1 < 2 || m->sa2 < 2) {
+        set_error("internal: TMEM budget exceeded for nrhs %d", k);
+        return DPCA_ERR_UNSUPPORTED;
+    }
     cudaError_t e;
     size_t om_elems = (size_t)N * h->n_ind_pad, bop_elems = (size_t)2 * N * h->n_snp_pad;
     if ((e = cudaMalloc(&m->omega_s, om_elems * 2)) != cudaSuccess ||
         (e = cudaMalloc(&m->bop, bop_elems * 2)) != cudaSuccess ||
         (e = cudaMalloc(&m->scales, 4 * (size_t)k * 8)) != cudaSuccess ||
-        (e = cudaMalloc(&m->rmax, 8)) != cudaSuccess) {
+        (e = cudaMalloc(&m->yt, (size_t)k * h->n_snp_pad * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&m->colmax, (size_t)k * 4)) != cudaSuccess) {
         set_error("mixed operand allocation: %s", cudaGetErrorString(e));
         return DPCA_ERR_NOMEM;
     }
@@ -463,10 +527,10 @@ dpca_status mixed_prepare(Handle *h) {
         set_error("mixed partial allocation: %s", cudaGetErrorString(e));
         return DPCA_ERR_NOMEM;
     }
-    m->sb1 = pick_sb(kXW, N);
-    m->sb2 = pick_sb(kXTY, N);
-    m->smem1 = smem_bytes(kXW, N, m->sb1, pick_sa(2 * N));
-    m->smem2 = smem_bytes(kXTY, N, m->sb2, pick_sa(N));
+    m->sb1 = pick_sb(kXW, N, m->kp);
+    m->sb2 = pick_sb(kXTY, N, m->kp);
+    m->smem1 = smem_bytes(kXW, N, m->kp, m->sb1, m->sa1);
+    m->smem2 = smem_bytes(kXTY, N, m->kp, m->sb2, m->sa2);
     DPCA_TRY(make_map(&m->map_p, CU_TENSOR_MAP_DATA_TYPE_UINT8, h->P, h->pitch, h->n_snp, h->pitch, 128, 128));
     DPCA_TRY(make_map(&m->map_pt, CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PT, h->pitchT, h->n_ind, h->pitchT, 128, 128));
     DPCA_TRY(make_map(&m->map_om, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, m->omega_s, h->n_ind_pad, N,
@@ -482,18 +546,11 @@ dpca_status mixed_prepare(Handle *h) {
 dpca_status mixed_release(Handle *h) {
     MixedState *m = mstate(h);
     if (!m) return DPCA_OK;
-    void *ptrs[] = {m->omega_s, m->bop, m->scales, m->rmax, m->partial};
+    void *ptrs[] = {m->omega_s, m->bop, m->yt, m->colmax, m->scales, m->partial};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete m;
     h->mx = nullptr;
-    return DPCA_OK;
-}
-
-dpca_status mixed_after_stats(Handle *h) {
-    MixedState *m = mstate(h);
-    rowbound_max_kernel<<<1, 1024, 0, h->stream>>>(h->rowbound, h->n_snp, m->rmax);
-    DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
 
@@ -502,7 +559,7 @@ dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out) {
     const int k = h->k, N = m->N;
     {
         ScopedLaunch t(&h->clock, h->stream, "split_omega");
-        omega_scales_kernel<<<k, 256, 0, h->stream>>>(omega, h->n_ind, k, m->rmax, m->scales);
+        omega_scales_kernel<<<k, 256, 0, h->stream>>>(omega, h->n_ind, k, m->scales);
         int64_t total = (int64_t)m->kp * h->n_ind_pad;
         int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 8);
         omega_split_kernel<<<grid, 256, 0, h->stream>>>(omega, h->n_ind, k, m->kp, h->n_ind_pad, m->scales,
@@ -516,17 +573,27 @@ dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out) {
     a.k = k;
     a.kp = m->kp;
     a.N = N;
-    a.sa = pick_sa(2 * N);
+    a.sa = m->sa1;
     a.sb = m->sb1;
     a.coef = h->coef;
     a.scales = m->scales;
-    a.bop = m->bop;
-    a.bop_ld = h->n_snp_pad;
+    a.yt = m->yt;
+    a.yt_ld = h->n_snp_pad;
+    a.colmax = m->colmax;
     a.y_out = y_out;
     a.err = h->dflag;
-    ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
-    mixed_gemm_kernel<kXW><<<dim3(ceil_div(h->n_snp, 128), 1), kThreads, m->smem1, h->stream>>>(m->map_p, m->map_om,
-                                                                                                 a);
+    DPCA_CUDA(cudaMemsetAsync(m->colmax, 0, (size_t)k * 4, h->stream));
+    {
+        ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
+        mixed_gemm_kernel<kXW><<<dim3(ceil_div(h->n_snp, 128), 1), kThreads, m->smem1, h->stream>>>(
+            m->map_p, m->map_om, a);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    ScopedLaunch t(&h->clock, h->stream, "split_bop");
+    int64_t total = (int64_t)k * h->n_snp;
+    int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 16);
+    bop_split_kernel<<<grid, 256, 0, h->stream>>>(m->yt, h->n_snp_pad, h->n_snp, k, m->kp, N, h->coef, m->colmax,
+                                                   m->scales, m->bop);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -541,7 +608,7 @@ dpca_status launch_mixed_xty(Handle *h, double *z) {
     a.k = k;
     a.kp = m->kp;
     a.N = N;
-    a.sa = pick_sa(N);
+    a.sa = m->sa2;
     a.sb = m->sb2;
     a.scales = m->scales;
     a.partial = m->partial;

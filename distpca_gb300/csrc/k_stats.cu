@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(256) snp_stats_kernel(const uint8_t *__restric
                                                         int n_snp, int64_t np, double inv_sqrt_nsnp,
                                                         int32_t *__restrict__ counts, double *__restrict__ avg,
                                                         double *__restrict__ sd, double *__restrict__ lut,
-                                                        double *__restrict__ coef, double *__restrict__ rowbound) {
+                                                        double *__restrict__ coef) {
     int lane = threadIdx.x & 31;
     int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (s >= n_snp) return;
@@ -58,15 +58,13 @@ __global__ void __launch_bounds__(256) snp_stats_kernel(const uint8_t *__restric
     double sdev = __dsqrt_rn(__dmul_rn(__dmul_rn(2.0, p), __dsub_rn(1.0, p)));
     avg[s] = mean;
     sd[s] = sdev;
-    double v00 = 0.0, v10 = 0.0, v11 = 0.0, b = 0.0, a = 0.0, rb = 0.0;
+    double v00 = 0.0, v10 = 0.0, v11 = 0.0, b = 0.0, a = 0.0;
     if (sdev > 1e-9) {
         v00 = __dmul_rn(__ddiv_rn(__dsub_rn(0.0, mean), sdev), inv_sqrt_nsnp);
         v10 = __dmul_rn(__ddiv_rn(__dsub_rn(1.0, mean), sdev), inv_sqrt_nsnp);
         v11 = __dmul_rn(__ddiv_rn(__dsub_rn(2.0, mean), sdev), inv_sqrt_nsnp);
         b = inv_sqrt_nsnp / sdev;
         a = -mean * b;
-        double nrm = sqrt((double)c00 * v00 * v00 + (double)c10 * v10 * v10 + (double)c11 * v11 * v11);
-        rb = fmax(fabs(a), fabs(b)) * nrm;
     }
     lut[4 * s + 0] = v00;
     lut[4 * s + 1] = 0.0;
@@ -76,7 +74,6 @@ __global__ void __launch_bounds__(256) snp_stats_kernel(const uint8_t *__restric
         coef[2 * s + 0] = b;
         coef[2 * s + 1] = a;
     }
-    if (rowbound) rowbound[s] = rb;
 }
 
 dpca_status launch_snp_stats(Handle *h) {
@@ -85,7 +82,7 @@ dpca_status launch_snp_stats(Handle *h) {
     int grid = ceil_div(h->n_snp, warps_per_block);
     snp_stats_kernel<<<grid, 32 * warps_per_block, 0, h->stream>>>(h->P, h->pitch, h->n_ind, h->n_snp, h->np,
                                                                      h->inv_sqrt_nsnp, h->counts, h->avg, h->sd,
-                                                                     h->lut, h->coef, h->rowbound);
+                                                                     h->lut, h->coef);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }

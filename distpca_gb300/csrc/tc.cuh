@@ -59,16 +59,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Wait until the phase with the given parity has completed.  Gives up (returns false) when
-// another thread has already flagged an error, or after kWaitCycles, recording `code`.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+// another thread has already flagged an error, or after kWaitCycles, recording `code`.  The
+// clock and the (global) error flag are read only every 256 polls so that the poll loop itself
+// stays off the handoff's critical path; `relaxed` waiters (roles with slack) back off with
+// nanosleep to leave issue slots to the latency-critical warps.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code, bool relaxed = false) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
-    while (true) {
+    for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (*(volatile int *)err) return false;
-        if (clock64() - t0 > kWaitCycles) {
-            atomicCAS(err, 0, code);
-            return false;
+        if (relaxed && it > 16) __nanosleep(64);
+        if ((it & 255u) == 0) {
+            if (*(volatile int *)err) return false;
+            if (clock64() - t0 > kWaitCycles) {
+                atomicCAS(err, 0, code);
+                return false;
+            }
         }
     }
 }

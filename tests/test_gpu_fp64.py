@@ -127,3 +127,17 @@ def test_unsupported_width_is_reported(dpca):
     with pytest.raises(dpca.DpcaError) as e:
         dpca.Handle(1000, 1000, 129)
     assert e.value.status == 6
+
+
+@pytest.mark.parametrize("k", [64, 96, 128])
+def test_wide_subspace_pass(dpca, oracle, k):
+    # widths whose shared-memory tiles pass the default 48 KB limit
+    prefix, n_ind, n_snp, packed = fileset("wide")
+    om = np.random.default_rng(k).standard_normal((n_ind, k))
+    zr, _ = oracle.one_pass(packed, n_ind, om, bsize=300)
+    with dpca.Handle(n_ind, n_snp, k, precision="fp64") as h:
+        h.upload(packed)
+        h.set_omega(om)
+        h.pass_()
+        z = h.z()
+    assert rel_max(z, zr) < 1e-12

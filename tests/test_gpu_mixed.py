@@ -1,10 +1,11 @@
 """The mixed-precision tcgen05 path against the oracle, the FP64 GPU path and the reference.
 
 Tolerances (written here, derived from the arithmetic): genotypes enter the
-tensor cores exactly; Omega and b.Y, a.Y carry 22 significant bits (hi + lo
-FP16 after a power-of-two column scale, ~2.4e-7 relative) and products
-accumulate in FP32.  One pass therefore agrees with the FP64 result to a few
-1e-7 of max|Z|; the test allows 2e-6.  Whole solves are held to the targets:
+tensor cores exactly; Omega and b.Y, a.Y are quantised to 24-bit fixed point per
+column (round to nearest, |error| <= 2^-24 of the column maximum) and every
+tensor-core sum is an exact integer, folded into FP64.  One pass therefore
+agrees with the FP64 result to about 2^-24 times the column max/rms ratio of
+the operands (~10 on these cohorts, ~6e-7 of max|Z|); the test allows 3e-6.  Whole solves are held to the targets:
 eigenvalues (sigma^2) within 1e-6 relative, largest principal angle of the
 nsv-dimensional PC subspace within 1e-4 rad, PC |corr| >= 0.999999 for the
 converged leading PCs.
@@ -37,11 +38,11 @@ def test_pass_matches_oracle(dpca, oracle, name, k):
     om = dpca.start_block(n_ind, k)
     zr, _ = oracle.one_pass(packed, n_ind, om, bsize=500)
     z = mixed_z(dpca, packed, n_ind, om)
-    assert rel_max(z, zr) < 2e-6
+    assert rel_max(z, zr) < 3e-6
 
 
 @pytest.mark.parametrize("n_ind,n_snp,k", [(5, 7, 2), (129, 513, 3), (517, 2049, 17), (1000, 3001, 40),
-                                           (2048, 4099, 64), (3001, 1500, 96), (64, 20000, 8)])
+                                           (2048, 4099, 48), (3001, 1500, 33), (64, 20000, 8)])
 def test_pass_ragged_shapes_vs_fp64(dpca, n_ind, n_snp, k):
     from distpca_gb300 import synth
 
@@ -55,7 +56,7 @@ def test_pass_ragged_shapes_vs_fp64(dpca, n_ind, n_snp, k):
         h.pass_()
         zf = h.z()
     z = mixed_z(dpca, packed, n_ind, om)
-    assert rel_max(z, zf) < 2e-6
+    assert rel_max(z, zf) < 3e-6
 
 
 def test_pass_deterministic(dpca):
@@ -109,13 +110,31 @@ def test_larger_pass_vs_fp64(dpca):
             h.pass_()
             out[prec] = h.z()
     err = rel_max(out["mixed"], out["fp64"])
-    assert err < 2e-6, err
-    # column-wise relative error of the dominant directions
+    assert err < 3e-6, err
+    # column-wise: the quantisation error is absolute (a fraction of each operand column's
+    # maximum), so columns of Z in the bulk of the spectrum, ~40x smaller than the largest
+    # ones, see a larger relative error
     col = np.linalg.norm(out["mixed"] - out["fp64"], axis=0) / np.linalg.norm(out["fp64"], axis=0)
-    assert col.max() < 2e-6, col
+    assert col.max() < 2e-5, col
+
+
+def test_larger_solve_accuracy_vs_fp64(dpca):
+    # the solve-level targets at a larger shape: eigenvalues within 1e-6 relative, PC subspace
+    # within 1e-4 rad of the FP64 GPU path, same start block and iteration schedule
+    from distpca_gb300 import synth
+
+    c = synth.make_cohort(20_000, 100_000, n_pop=8, dirichlet=True, fst=0.02, p_range=(0.01, 0.5), missing=0.02,
+                          seed=2)
+    packed = synth.pack_rows(c)
+    kw = dict(nsv=10, nrhs=20, power=2, crit=1, tol=1e-6, miter=30, bsize=10_000, verbose=0)
+    rf = dpca.run_packed(packed, c.n_ind, precision="fp64", **kw)
+    rm = dpca.run_packed(packed, c.n_ind, precision="mixed", **kw)
+    lam_f, lam_m = rf["sigma"] ** 2, rm["sigma"] ** 2
+    assert np.max(np.abs(lam_m - lam_f) / lam_f) < 1e-6
+    assert subspace_angle(rm["u"], rf["u"]) < 1e-4
 
 
 def test_mixed_width_limit(dpca):
     with pytest.raises(dpca.DpcaError) as e:
-        dpca.Handle(1000, 1000, 97, precision="mixed")
+        dpca.Handle(1000, 1000, 49, precision="mixed")
     assert e.value.status == 6
