@@ -17,9 +17,10 @@
 //     h, l in [-2048, 2048] (FP16 holds every such integer exactly), laid side by side along the
 //     MMA's N dimension ([h | l], N = 2*round_up(k, 8));
 //   - a TMEM accumulator sums at most kChunkXW (resp. kChunkXTY) K-blocks, which bounds every
-//     partial sum below 2^24, then four accumulator warps fold it into FP64 (in shared memory)
-//     while the tensor core fills the other of two accumulator sets.
-// The per-SNP coefficients, the slice recombination and the scale removal run in FP64.  The
+//     partial sum below 2^24, then four accumulator warps fold it, as the exact integer
+//     4096 h + l, into 64-bit integer accumulators in shared memory while the tensor core fills
+//     the other of two accumulator sets.
+// The per-SNP coefficients and the scale removal are applied once per output, in FP64.  The
 // X Omega epilogue writes Y (FP32, transposed) and the exact column maxima of |b.Y|, |a.Y|, from
 // which a split kernel quantises the X^T Y operand.
 //
@@ -123,8 +124,12 @@ __device__ __forceinline__ void fixed_slices(double v, __half &hi, __half &lo) {
     lo = __double2half(n - 4096.0 * h);  // exact: |l| <= 2048
 }
 
-__device__ __forceinline__ double slices_value(uint32_t hbits, uint32_t lbits) {
-    return 4096.0 * (double)__uint_as_float(hbits) + (double)__uint_as_float(lbits);
+// An accumulator pair (h slice, l slice) of one chunk -> the exact integer 4096 h + l.  Both halves
+// are integers below 2^24 in FP32, so the conversions are exact; the fold stays in integer
+// arithmetic (FP64 throughput is a small fraction of the integer pipes').
+__device__ __forceinline__ long long slices_int(uint32_t hbits, uint32_t lbits) {
+    return (long long)__float2int_rz(__uint_as_float(hbits)) * 4096LL +
+           (long long)__float2int_rz(__uint_as_float(lbits));
 }
 
 template <int MODE>
@@ -138,8 +143,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int bstage = (MODE == kXW ? 1 : 2) * N * 128;
     uint8_t *sP = smem;
     uint8_t *sB = smem + kPStages * kPStageBytes;
-    double *acc64 = (double *)(sB + (size_t)SB * bstage);  // [kp][128] FP64 accumulators
-    uint64_t *bars = (uint64_t *)(acc64 + (size_t)kp * 128);
+    // exact accumulators, [parts][kp][128]: X Omega keeps the G' and M products apart (their
+    // per-SNP coefficients differ), X^T Y sums both (coefficients are inside its operand)
+    constexpr int kParts = MODE == kXW ? 2 : 1;
+    long long *acc = (long long *)(sB + (size_t)SB * bstage);
+    uint64_t *bars = (uint64_t *)(acc + (size_t)kParts * kp * 128);
     uint64_t *pk_full = bars, *pk_empty = bars + kPStages;
     uint64_t *b_full = pk_empty + kPStages, *b_empty = b_full + SB;
     uint64_t *a_full = b_empty + SB, *a_empty = a_full + SA;
@@ -193,25 +201,27 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         // ---------------------------------------------------------- TMA producer
         if (lane == 0) {
-            int issued_p = 0, issued_b = 0;
+            // ring positions advance incrementally: the stage counts are runtime values, and a
+            // division per K-block would sit on this thread's critical path
+            int sp = 0, sb = 0, issued_p = 0, issued_b = 0;
+            uint32_t pph = 0, bph = 0;
             bool ok = true;
             for (int g = 0; g < npg && ok; ++g) {
-                const int sp = g % kPStages;
-                ok = tc::mbar_wait(&pk_empty[sp], ((g / kPStages) & 1) ^ 1, err, 11, true);
+                ok = tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true);
                 if (!ok) break;
                 tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
                 tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (kb0 + 8 * g) * 16, tile * 128);
                 issued_p = g + 1;
+                if (++sp == kPStages) sp = 0, pph ^= 1;
                 const int jn = min(8, nkb - 8 * g);
                 for (int j = 0; j < jn; ++j) {
-                    const int kb = 8 * g + j, sb = kb % SB;
-                    ok = tc::mbar_wait(&b_empty[sb], ((kb / SB) & 1) ^ 1, err, 12, true);
+                    ok = tc::mbar_wait(&b_empty[sb], bph ^ 1, err, 12, true);
                     if (!ok) break;
                     tc::mbar_arrive_expect_tx(&b_full[sb], bstage);
-                    uint8_t *dst = sB + (size_t)sb * bstage;
-                    tc::tma_load_2d(dst, &map_b, &b_full[sb], (kb0 + kb) * 64, 0);
-                    if (MODE == kXTY) tc::tma_load_2d(dst + N * 128, &map_b, &b_full[sb], (kb0 + kb) * 64, N);
-                    issued_b = kb + 1;
+                    // one box per stage: X Omega N rows, X^T Y 2N rows ([b.Y | a.Y] slices)
+                    tc::tma_load_2d(sB + (size_t)sb * bstage, &map_b, &b_full[sb], (kb0 + 8 * g + j) * 64, 0);
+                    issued_b = 8 * g + j + 1;
+                    if (++sb == SB) sb = 0, bph ^= 1;
                 }
             }
             // drain: every issued copy must land before the CTA may exit
@@ -230,24 +240,30 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t bdesc0 =
                 tc::desc_kmajor_sw128(tc::smem_u32(sB) + (MODE == kXTY ? (uint32_t)(v * N * 128) : 0u));
             const uint32_t a_v = tbase + a_col(0, v);
+            int sb = 0, sa = 0, kc = 0, chunk = 0;
+            uint32_t bph = 0, aph = 0;
             for (int kb = 0; kb < nkb; ++kb) {
-                const int chunk = kb / kChunk, set = chunk & 1;
-                const bool first = (kb % kChunk) == 0;
-                if (first && chunk >= 2 && !tc::mbar_wait(&acc_empty[set], ((chunk >> 1) - 1) & 1, err, 23)) break;
-                const int sb = kb % SB, sa = kb % SA;
-                if (!tc::mbar_wait(&b_full[sb], (kb / SB) & 1, err, 21)) break;
-                if (!tc::mbar_wait(&a_full[sa], (kb / SA) & 1, err, 22)) break;
+                const int set = chunk & 1;
+                if (kc == 0 && chunk >= 2 && !tc::mbar_wait(&acc_empty[set], ((chunk >> 1) - 1) & 1, err, 23)) break;
+                if (!tc::mbar_wait(&b_full[sb], bph, err, 21)) break;
+                if (!tc::mbar_wait(&a_full[sa], aph, err, 22)) break;
                 tc::fence_after_sync();
                 const uint64_t bd = bdesc0 + (uint64_t)((sb * bstage) >> 4);
                 const uint32_t d = tbase + (uint32_t)(set * set_cols + v * N);
                 const uint32_t a = a_v + (uint32_t)(64 * sa);
-                tc::mma_ts_f16(d, a, bd, idesc, first ? 0u : 1u);
+                tc::mma_ts_f16(d, a, bd, idesc, kc == 0 ? 0u : 1u);
                 tc::mma_ts_f16(d, a + 8, bd + 2, idesc, 1u);
                 tc::mma_ts_f16(d, a + 16, bd + 4, idesc, 1u);
                 tc::mma_ts_f16(d, a + 24, bd + 6, idesc, 1u);
                 tc::mma_commit(&b_empty[sb]);
                 tc::mma_commit(&a_empty[sa]);
-                if ((kb % kChunk) == kChunk - 1 || kb == nkb - 1) tc::mma_commit(&acc_full[set]);
+                if (++kc == kChunk || kb == nkb - 1) {
+                    tc::mma_commit(&acc_full[set]);
+                    kc = 0;
+                    ++chunk;
+                }
+                if (++sb == SB) sb = 0, bph ^= 1;
+                if (++sa == SA) sa = 0, aph ^= 1;
             }
         }
     } else if (warp >= 2 && warp < 2 + 4 * kDecodeGroups) {
@@ -257,11 +273,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int r = 32 * q + lane;
         const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
         uint32_t G[32], M[32];
+        int sa = grp % SA;
+        uint32_t aph = (uint32_t)(grp / SA) & 1u;
         for (int kb = grp; kb < nkb; kb += kDecodeGroups) {
-            const int g = kb >> 3, j = kb & 7, sp = g % kPStages, sa = kb % SA;
+            const int g = kb >> 3, j = kb & 7, sp = g % kPStages;
             bool ok = tc::mbar_wait(&pk_full[sp], (g / kPStages) & 1, err, 31);
-            ok = ok && tc::mbar_wait(&a_empty[sa], ((kb / SA) & 1) ^ 1, err, 32);
+            ok = ok && tc::mbar_wait(&a_empty[sa], aph ^ 1, err, 32);
             if (!__all_sync(0xffffffffu, ok)) break;  // TMEM stores below are warp-collective
+            tc::fence_after_sync();
             const uint4 v = *reinterpret_cast<const uint4 *>(sP + sp * kPStageBytes + r * 128 + ((j ^ (r & 7)) << 4));
             decode64(v, G, M);
             tc::tmem_st_x32(lane_base + a_col(sa, 0), G);
@@ -271,6 +290,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::mbar_arrive(&a_full[sa]);
             // last K-block of this group inside the packed stage: release the stage
             if (kb + kDecodeGroups > min(8 * g + 7, nkb - 1)) tc::mbar_arrive(&pk_empty[sp]);
+            sa += kDecodeGroups;  // SA >= kDecodeGroups: one wrap at most
+            if (sa >= SA) sa -= SA, aph ^= 1;
         }
     } else if (warp < 14) {
         // ---------------------------------------------------------- accumulate (warps 10..13)
@@ -284,7 +305,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             b = args.coef[2 * (size_t)row];
             a = args.coef[2 * (size_t)row + 1];
         }
-        for (int c = 0; c < kp; ++c) acc64[c * 128 + r] = 0.0;
+        for (int c = 0; c < kParts * kp; ++c) acc[c * 128 + r] = 0;
         bool ok = true;
         for (int chunk = 0; chunk < nchunks; ++chunk) {
             const int set = chunk & 1;
@@ -293,26 +314,21 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::fence_after_sync();
             const uint32_t cb = lane_base + (uint32_t)(set * set_cols);
             for (int c0 = 0; c0 < kp; c0 += 8) {
-                if (MODE == kXW) {
-                    uint32_t gh[8], gl[8], mh[8], ml[8];
-                    tc::tmem_ld_x8(cb + c0, gh);
-                    tc::tmem_ld_x8(cb + kp + c0, gl);
-                    tc::tmem_ld_x8(cb + N + c0, mh);
-                    tc::tmem_ld_x8(cb + N + kp + c0, ml);
-                    tc::tmem_wait_ld();
+                uint32_t gh[8], gl[8], mh[8], ml[8];
+                tc::tmem_ld_x8(cb + c0, gh);
+                tc::tmem_ld_x8(cb + kp + c0, gl);
+                tc::tmem_ld_x8(cb + N + c0, mh);
+                tc::tmem_ld_x8(cb + N + kp + c0, ml);
+                tc::tmem_wait_ld();
 #pragma unroll
-                    for (int jj = 0; jj < 8; ++jj)
-                        acc64[(c0 + jj) * 128 + r] += b * slices_value(gh[jj], gl[jj]) + a * slices_value(mh[jj], ml[jj]);
-                } else {
-                    uint32_t gh[8], gl[8], mh[8], ml[8];
-                    tc::tmem_ld_x8(cb + c0, gh);
-                    tc::tmem_ld_x8(cb + kp + c0, gl);
-                    tc::tmem_ld_x8(cb + N + c0, mh);
-                    tc::tmem_ld_x8(cb + N + kp + c0, ml);
-                    tc::tmem_wait_ld();
-#pragma unroll
-                    for (int jj = 0; jj < 8; ++jj)
-                        acc64[(c0 + jj) * 128 + r] += slices_value(gh[jj], gl[jj]) + slices_value(mh[jj], ml[jj]);
+                for (int jj = 0; jj < 8; ++jj) {
+                    const long long vg = slices_int(gh[jj], gl[jj]), vm = slices_int(mh[jj], ml[jj]);
+                    if (MODE == kXW) {
+                        acc[(c0 + jj) * 128 + r] += vg;
+                        acc[(kp + c0 + jj) * 128 + r] += vm;
+                    } else {
+                        acc[(c0 + jj) * 128 + r] += vg + vm;
+                    }
                 }
             }
             tc::fence_before_sync();
@@ -324,7 +340,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int c = 0; c < k; ++c) {
                 float mag = 0.f;
                 if (valid) {
-                    const double y = acc64[c * 128 + r] * sc[k + c];
+                    const double y =
+                        (b * (double)acc[c * 128 + r] + a * (double)acc[(kp + c) * 128 + r]) * sc[k + c];
                     if (args.y_out) args.y_out[(size_t)row * k + c] = y;
                     args.yt[(int64_t)c * args.yt_ld + row] = (float)y;
                     mag = (float)(fmax(fabs(b), fabs(a)) * fabs(y));
@@ -335,7 +352,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         } else if (valid) {
             double *out = args.partial + ((size_t)split * args.rows + row) * k;
-            for (int c = 0; c < k; ++c) out[c] = acc64[c * 128 + r] * sc[3 * k + c];
+            for (int c = 0; c < k; ++c) out[c] = (double)acc[c * 128 + r] * sc[3 * k + c];
         }
     }
     tc::fence_before_sync();
@@ -460,14 +477,16 @@ static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base
 
 static MixedState *mstate(Handle *h) { return (MixedState *)h->mx; }
 
+static size_t acc_bytes(int mode, int kp) { return (size_t)(mode == kXW ? 2 : 1) * kp * 128 * 8; }
+
 static size_t smem_bytes(int mode, int N, int kp, int sb, int sa) {
     size_t b = 1024 + (size_t)kPStages * kPStageBytes + (size_t)sb * (mode == kXW ? 1 : 2) * N * 128 +
-               (size_t)kp * 128 * 8 + (size_t)(2 * kPStages + 2 * sb + 2 * sa + 4) * 8 + 16;
+               acc_bytes(mode, kp) + (size_t)(2 * kPStages + 2 * sb + 2 * sa + 4) * 8 + 16;
     return std::max<size_t>(b, kSmemFloor);
 }
 
 static int pick_sb(int mode, int N, int kp) {
-    const size_t budget = 210 * 1024 - (size_t)kPStages * kPStageBytes - (size_t)kp * 128 * 8;
+    const size_t budget = 210 * 1024 - (size_t)kPStages * kPStageBytes - acc_bytes(mode, kp);
     int sb = (int)(budget / ((size_t)(mode == kXW ? 1 : 2) * N * 128));
     return std::max(2, std::min(8, sb));
 }
@@ -536,7 +555,7 @@ dpca_status mixed_prepare(Handle *h) {
     DPCA_TRY(make_map(&m->map_om, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, m->omega_s, h->n_ind_pad, N,
                       (uint64_t)h->n_ind_pad * 2, 64, N));
     DPCA_TRY(make_map(&m->map_bop, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, m->bop, h->n_snp_pad, 2 * N,
-                      (uint64_t)h->n_snp_pad * 2, 64, N));
+                      (uint64_t)h->n_snp_pad * 2, 64, 2 * N));
     DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem1));
     DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)m->smem2));
