@@ -16,27 +16,34 @@
 //     point, an unbiased quantisation), stored as two integer FP16 slices v = 4096 h + l with
 //     h, l in [-2048, 2048] (FP16 holds every such integer exactly), laid side by side along the
 //     MMA's N dimension ([h | l], N = 2*round_up(k, 8));
-//   - a TMEM accumulator sums at most kChunkXW (resp. kChunkXTY) K-blocks, which bounds every
-//     partial sum below 2^24, then four accumulator warps fold it, as the exact integer
-//     4096 h + l, into 64-bit integer accumulators in shared memory while the tensor core fills
-//     the other of two accumulator sets.
+//   - the G' and M products have one TMEM accumulator each; an accumulator sums a bounded
+//     number of K-blocks (a chunk) so that every partial sum stays within 2^24, then the drain
+//     warps copy it to registers, release it, and fold the exact integer 4096 h + l into 64-bit
+//     integer accumulators in shared memory.  The M chunks end half a G' chunk later than the
+//     G' chunks, so the tensor core keeps working on one product while the other is drained.
 // The per-SNP coefficients and the scale removal are applied once per output, in FP64.  The
 // X Omega epilogue writes Y (FP32, transposed) and the exact column maxima of |b.Y|, |a.Y|, from
 // which a split kernel quantises the X^T Y operand.
 //
+// Pipeline step = one batch of two 64-element K-blocks (8 MMA K-steps per product).  Batching
+// matters: an MMA-issuing thread spends ~150 cycles on each barrier wait and ~45 on each
+// instruction it issues, against 40 tensor-core cycles per M=128, N=80, K=16 MMA, so a wait and
+// a commit must be spread over at least eight MMAs per issuer to keep the tensor core busy.
+//
 // CTA structure (one CTA per 128-row output tile and K split, 480 threads, 1 CTA per SM):
-//   warp 0       TMA producer: packed 2-bit tiles [128 rows x 128 B] and FP16 slice tiles
-//                [N rows x 64 elements], both 128-byte swizzled.
+//   warp 0       TMA producer: packed 2-bit tiles [128 rows x 128 B] (4 batches) and one 3-D
+//                box of FP16 slice tiles per batch [2 K-blocks][rows][64 elements], 128-byte
+//                swizzled.
 //   warps 1, 14  TMEM allocation (warp 1) and the two MMA-issuing threads
 //                (tcgen05.mma.kind::f16, A from tensor memory, B from shared memory): warp 1
-//                issues the G' products, warp 14 the M products, each into its own accumulator,
-//                because one thread cannot issue N=80 MMAs as fast as the tensor core runs them.
-//   warps 2..9   decode, two groups of four warps on alternating K-blocks: one thread per tile
-//                row turns 16 packed bytes (64 genotypes) into 32+32 FP16 pairs with
-//                byte-permute table lookups and stores them into TMEM (tcgen05.st).
-//   warps 10..13 accumulate: drain finished TMEM accumulator chunks (tcgen05.ld) into FP64 and
-//                write the outputs.
-// Pipelines are mbarrier rings; every wait is bounded (tc.cuh) and reports through h->dflag.
+//                issues the G' products, warp 14 the M products, each into its own accumulator.
+//   warps 2..9   decode, two groups of four warps, each owning one TMEM A stage and taking
+//                alternate batches: one thread per tile row turns 2 x 16 packed bytes into
+//                FP16 pairs with byte-permute table lookups and stores them (tcgen05.st).
+//   warps 10..13 drain: accumulator chunks (tcgen05.ld) into exact 64-bit integers; outputs.
+// Barriers per batch: one "full" (TMA bytes + the decode group) and one "free" (both issuers'
+// commits), so each issuer waits once and commits once per batch.  Every wait is bounded
+// (tc.cuh) and reports through h->dflag.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -53,25 +60,27 @@ constexpr int kXTY = 2;  // Z = X^T Y   (rows = individuals, K = SNPs)
 constexpr int kWarps = 15;
 constexpr int kIssuerWarpM = 14;
 constexpr int kThreads = 32 * kWarps;
-constexpr int kDecodeGroups = 2;
+constexpr int kDecodeGroups = 2;         // one TMEM A stage per group
 constexpr int kPStages = 3;
-constexpr int kPStageBytes = 128 * 128;  // 128 rows x 128 B = 512 K-elements = 8 K-blocks
+constexpr int kPStageBytes = 128 * 128;  // 128 rows x 128 B = 512 K-elements = 8 K-blocks = 4 batches
 constexpr int kTmemCols = 512;
 constexpr int kSmemFloor = 120 * 1024;   // keeps one CTA per SM (the CTA owns all of TMEM)
-// K-blocks per exact accumulation chunk.  One K step (16 products) adds at most 16*2*2048 = 2^16
-// to an X Omega accumulator and 16*(2+1)*2048 = 1.5*2^16 to an X^T Y accumulator; chunks keep
-// |partial sum| + one step's products below 2^24 (48*4 = 192 and 32*4 = 128 steps), so every
-// intermediate value is an integer the FP32 accumulator holds exactly.
-constexpr int kChunkXW = 48;
-constexpr int kChunkXTY = 32;
-constexpr int kMaxMixedNrhs = 48;        // two accumulator sets of 2 x N columns fit TMEM
+constexpr int kSmemBudget = 220 * 1024;
+// Batches per exact accumulation chunk.  A batch is 8 K steps of 16 products; a G' product
+// term is at most 2 * 2048 in magnitude, so a batch adds at most 2^19 and 32 batches at most
+// 2^24; an M term is at most 2048, allowing 64 batches.  Every partial sum is then an integer
+// of magnitude <= 2^24, which the FP32 accumulator holds exactly whatever the summation order.
+constexpr int kChunkG = 32;
+constexpr int kChunkM = 64;
+constexpr int kFirstChunkM = 48;         // staggers the M drains against the G' drains
+constexpr int kMaxMixedNrhs = 48;        // accumulators 2 x N <= 192 columns + 2 A stages of 128
 
 struct GemmArgs {
     int rows;          // valid output rows
     int nkb_total;     // 64-element K blocks covering K
     int kb_per_split;  // K blocks per CTA (multiple of 8)
     int k, kp, N;
-    int sa, sb;        // A stages (TMEM), B stages (SMEM)
+    int ring;          // batches in flight (B stages in shared memory)
     const double *coef;     // kXW: [rows][2] {b, a}
     const double *scales;   // [4][k]: omega scale, its inverse, b/aY scale, its inverse
     float *yt;              // kXW: Y transposed, [k][yt_ld] (FP32)
@@ -91,29 +100,38 @@ struct MixedState {
     double *scales = nullptr;   // [4][k]
     double *partial = nullptr;  // [splits][n_ind][k]
     int splits = 1, kb_per_split = 8;
-    int sb1 = 2, sb2 = 2, sa1 = 2, sa2 = 2;
+    int ring1 = 2, ring2 = 2;
     size_t smem1 = 0, smem2 = 0;
     CUtensorMap map_p, map_pt, map_om, map_bop;
 };
 
 // ------------------------------------------------------------------ decode
-// 16 packed bytes = 64 codes -> FP16 pairs: G[m] holds g' of elements (2m, 2m+1), M[m] the
-// non-missing indicator.  Per pair of codes (c0 low, c1 high) the selector picks, for the
-// high byte of each half, entry c of a 4-byte table; the low bytes select a zero byte.
+// K order inside every 16-element group.  Pair register p of a 32-bit word of 16 codes holds
+// the codes at positions a_p and a_p + 4, a_p = (p & 3) + 8 (p >> 2), so that one shift of the
+// word puts both codes where the byte-permute selector needs them (bits 4-5 and 12-13).  The
+// dense operands are stored in the same order: logical K position L of a group holds element
+// perm16(L) of that group.
+__host__ __device__ __forceinline__ int perm16(int L) { return ((L >> 1) & 3) + 8 * (L >> 3) + 4 * (L & 1); }
+
+// 16 packed bytes = 64 codes -> FP16 pairs: G[8q + p] holds g' of the pair (a_p, a_p + 4) of
+// word q, M[8q + p] the non-missing indicator.  The selector picks, for the high byte of each
+// half, entry c of a 4-byte table; the low bytes select a zero byte.
 //   g': 00 -> 0, 01 (missing) -> 0, 10 -> 1.0 (0x3C00), 11 -> 2.0 (0x4000)
 //   m : 00 -> 1, 01 -> 0,           10 -> 1,             11 -> 1
 __device__ __forceinline__ void decode64(uint4 v, uint32_t (&G)[32], uint32_t (&M)[32]) {
     const uint32_t TG = 0x403C0000u, TM = 0x3C3C003Cu;
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < 4; ++q) {
+        const uint32_t x = w[q];
+        const uint32_t sh[8] = {x << 4, x << 2, x, x >> 2, x >> 12, x >> 14, x >> 16, x >> 18};
 #pragma unroll
         for (int p = 0; p < 8; ++p) {
-            uint32_t u = (w[q] >> (4 * p)) & 0xFu;
-            uint32_t sel = ((u * 0x410u) & 0x3030u) | 0x0404u;
+            const uint32_t sel = (sh[p] & 0x3030u) | 0x0404u;
             G[q * 8 + p] = __byte_perm(TG, 0u, sel);
             M[q * 8 + p] = __byte_perm(TM, 0u, sel);
         }
+    }
 }
 
 // v (already scaled, |v| < 2^23) -> nearest integer n = 4096 h + l, h and l in [-2048, 2048].
@@ -132,52 +150,66 @@ __device__ __forceinline__ long long slices_int(uint32_t hbits, uint32_t lbits) 
            (long long)__float2int_rz(__uint_as_float(lbits));
 }
 
+// Slow path of a wait, out of line so that the MMA issue loop stays compact (an inlined wait
+// loop in that loop costs ~90 cycles per iteration even when it never runs).
+__device__ __noinline__ bool wait_slow(uint64_t *bar, uint32_t parity, int *err, int code) {
+    return tc::mbar_wait(bar, parity, err, code);
+}
+
+__device__ __forceinline__ bool wait_fast(uint64_t *bar, uint32_t parity, int *err, int code) {
+    return tc::mbar_try_wait(bar, parity) || wait_slow(bar, parity, err, code);
+}
+
+// Chunks of an accumulator whose first chunk has `first` batches and the others `len`.
+__device__ __forceinline__ int chunk_count(int nb, int first, int len) {
+    return nb <= first ? 1 : 1 + (nb - first + len - 1) / len;
+}
+
+__device__ __forceinline__ int chunk_end(int c, int nb, int first, int len) {
+    return min(first - 1 + c * len, nb - 1);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     mixed_gemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                       const GemmArgs args) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const int N = args.N, kp = args.kp, SA = args.sa, SB = args.sb;
-    constexpr int kChunk = MODE == kXW ? kChunkXW : kChunkXTY;
-    const int bstage = (MODE == kXW ? 1 : 2) * N * 128;
+    const int N = args.N, kp = args.kp, R = args.ring;
+    const int rows_box = (MODE == kXW ? 1 : 2) * N;  // B rows per K-block tile
+    const int tile_bytes = rows_box * 128;
+    const int bstage = 2 * tile_bytes;                // one batch
     uint8_t *sP = smem;
     uint8_t *sB = smem + kPStages * kPStageBytes;
     // exact accumulators, [parts][kp][128]: X Omega keeps the G' and M products apart (their
     // per-SNP coefficients differ), X^T Y sums both (coefficients are inside its operand)
     constexpr int kParts = MODE == kXW ? 2 : 1;
-    long long *acc = (long long *)(sB + (size_t)SB * bstage);
+    long long *acc = (long long *)(sB + (size_t)R * bstage);
     uint64_t *bars = (uint64_t *)(acc + (size_t)kParts * kp * 128);
     uint64_t *pk_full = bars, *pk_empty = bars + kPStages;
-    uint64_t *b_full = pk_empty + kPStages, *b_empty = b_full + SB;
-    uint64_t *a_full = b_empty + SB, *a_empty = a_full + SA;
-    uint64_t *acc_full = a_empty + SA, *acc_empty = acc_full + 2;
+    uint64_t *full = pk_empty + kPStages, *free_ = full + R;
+    uint64_t *acc_full = free_ + R, *acc_empty = acc_full + 2;
     uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x, split = blockIdx.y;
     const int kb0 = split * args.kb_per_split;
     const int nkb = min(args.nkb_total, kb0 + args.kb_per_split) - kb0;
-    const int npg = (nkb + 7) >> 3;
-    const int nchunks = (nkb + kChunk - 1) / kChunk;
+    const int nb = (nkb + 1) >> 1;  // a trailing half batch reads zero operand columns
     int *err = args.err;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kPStages; ++s) {
             tc::mbar_init(&pk_full[s], 1);
-            tc::mbar_init(&pk_empty[s], 128 * kDecodeGroups);
+            tc::mbar_init(&pk_empty[s], 4 * kDecodeGroups);  // one elected lane per decode warp
         }
-        for (int s = 0; s < SB; ++s) {
-            tc::mbar_init(&b_full[s], 1);
-            tc::mbar_init(&b_empty[s], 2);  // one commit per MMA issuer
+        for (int s = 0; s < R; ++s) {
+            tc::mbar_init(&full[s], 1 + 4);  // producer (with the TMA bytes) + 4 decode warps
+            tc::mbar_init(&free_[s], 2);     // one commit per MMA issuer
         }
-        for (int s = 0; s < SA; ++s) {
-            tc::mbar_init(&a_full[s], 128);
-            tc::mbar_init(&a_empty[s], 2);
-        }
-        for (int s = 0; s < 2; ++s) {
-            tc::mbar_init(&acc_full[s], 2);
-            tc::mbar_init(&acc_empty[s], 128);
+        for (int v = 0; v < 2; ++v) {
+            tc::mbar_init(&acc_full[v], 1);
+            tc::mbar_init(&acc_empty[v], 4);
         }
         tc::fence_mbar_init();
         tc::tma_prefetch(&map_a);
@@ -191,79 +223,74 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = *tmem_slot;
-    // TMEM columns: accumulator set s at [s * set_cols, (s+1) * set_cols) -- the G' products'
-    // [h | l] block, then the M products' -- then the A stages (32 columns per variant) from a
-    // 32-column boundary.
-    const int set_cols = 2 * N;
-    const int a_base = (2 * set_cols + 31) & ~31;
-    auto a_col = [&](int stage, int variant) -> uint32_t { return (uint32_t)(a_base + 64 * stage + 32 * variant); };
+    // TMEM columns: G' accumulator [0, N), M accumulator [N, 2N) (each [h | l] slices), then
+    // the two A stages (decode group g owns [a_base + 128 g, +128): G' K-blocks 0-1, then M).
+    const int a_base = (2 * N + 31) & ~31;
 
     if (warp == 0) {
         // ---------------------------------------------------------- TMA producer
         if (lane == 0) {
-            // ring positions advance incrementally: the stage counts are runtime values, and a
-            // division per K-block would sit on this thread's critical path
-            int sp = 0, sb = 0, issued_p = 0, issued_b = 0;
+            int sp = 0, r = 0, issued_p = 0, issued_b = 0;
             uint32_t pph = 0, bph = 0;
-            bool ok = true;
-            for (int g = 0; g < npg && ok; ++g) {
-                ok = tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true);
-                if (!ok) break;
-                tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
-                tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (kb0 + 8 * g) * 16, tile * 128);
-                issued_p = g + 1;
-                if (++sp == kPStages) sp = 0, pph ^= 1;
-                const int jn = min(8, nkb - 8 * g);
-                for (int j = 0; j < jn; ++j) {
-                    ok = tc::mbar_wait(&b_empty[sb], bph ^ 1, err, 12, true);
-                    if (!ok) break;
-                    tc::mbar_arrive_expect_tx(&b_full[sb], bstage);
-                    // one box per stage: X Omega N rows, X^T Y 2N rows ([b.Y | a.Y] slices)
-                    tc::tma_load_2d(sB + (size_t)sb * bstage, &map_b, &b_full[sb], (kb0 + 8 * g + j) * 64, 0);
-                    issued_b = 8 * g + j + 1;
-                    if (++sb == SB) sb = 0, bph ^= 1;
+            for (int t = 0; t < nb; ++t) {
+                if ((t & 3) == 0) {
+                    if (!tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true)) break;
+                    tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
+                    tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (kb0 + 2 * t) * 16, tile * 128);
+                    issued_p = (t >> 2) + 1;
+                    if (++sp == kPStages) sp = 0, pph ^= 1;
                 }
+                if (!tc::mbar_wait(&free_[r], bph ^ 1, err, 12, true)) break;
+                tc::mbar_arrive_expect_tx(&full[r], bstage);
+                tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, 0, kb0 + 2 * t);
+                issued_b = t + 1;
+                if (++r == R) r = 0, bph ^= 1;
             }
             // drain: every issued copy must land before the CTA may exit
             for (int g = max(0, issued_p - kPStages); g < issued_p; ++g)
                 tc::mbar_wait(&pk_full[g % kPStages], (g / kPStages) & 1, err, 13, true);
-            for (int kb = max(0, issued_b - SB); kb < issued_b; ++kb)
-                tc::mbar_wait(&b_full[kb % SB], (kb / SB) & 1, err, 14, true);
+            for (int t = max(0, issued_b - R); t < issued_b; ++t)
+                tc::mbar_wait(&full[t % R], (t / R) & 1, err, 14, true);
         }
     } else if (warp == 1 || warp == kIssuerWarpM) {
         // ---------------------------------------------------------- MMA issuers
         if (lane == 0) {
             const int v = warp == 1 ? 0 : 1;  // 0: G' products, 1: M products
+            const int first_len = v ? kFirstChunkM : kChunkG, len = v ? kChunkM : kChunkG;
             const uint32_t idesc = tc::idesc_f16_f32(128, N);
-            // descriptor of B stage 0 (for X^T Y the M products use the stage's second half);
-            // a stage is bstage bytes further, a K step 32 bytes = 2 descriptor units
+            // B stage r, K-block j, K step s: stage base + j * tile_bytes (+ N rows for the X^T Y
+            // M products) + 32 s bytes; descriptors count 16-byte units
             const uint64_t bdesc0 =
                 tc::desc_kmajor_sw128(tc::smem_u32(sB) + (MODE == kXTY ? (uint32_t)(v * N * 128) : 0u));
-            const uint32_t a_v = tbase + a_col(0, v);
-            int sb = 0, sa = 0, kc = 0, chunk = 0;
-            uint32_t bph = 0, aph = 0;
-            for (int kb = 0; kb < nkb; ++kb) {
-                const int set = chunk & 1;
-                if (kc == 0 && chunk >= 2 && !tc::mbar_wait(&acc_empty[set], ((chunk >> 1) - 1) & 1, err, 23)) break;
-                if (!tc::mbar_wait(&b_full[sb], bph, err, 21)) break;
-                if (!tc::mbar_wait(&a_full[sa], aph, err, 22)) break;
+            const uint64_t tile_units = (uint64_t)(tile_bytes >> 4);
+            const uint32_t d = tbase + (uint32_t)(v * N);
+            const uint32_t a_v = tbase + (uint32_t)(a_base + 64 * v);
+            int r = 0, left = first_len, chunk = 0;
+            uint32_t ph = 0;
+            bool fresh = true;
+            for (int t = 0; t < nb; ++t) {
+                if (!wait_fast(&full[r], ph, err, 21)) break;
+                if (fresh && chunk > 0 && !wait_fast(&acc_empty[v], (chunk - 1) & 1, err, 22)) break;
                 tc::fence_after_sync();
-                const uint64_t bd = bdesc0 + (uint64_t)((sb * bstage) >> 4);
-                const uint32_t d = tbase + (uint32_t)(set * set_cols + v * N);
-                const uint32_t a = a_v + (uint32_t)(64 * sa);
-                tc::mma_ts_f16(d, a, bd, idesc, kc == 0 ? 0u : 1u);
-                tc::mma_ts_f16(d, a + 8, bd + 2, idesc, 1u);
-                tc::mma_ts_f16(d, a + 16, bd + 4, idesc, 1u);
-                tc::mma_ts_f16(d, a + 24, bd + 6, idesc, 1u);
-                tc::mma_commit(&b_empty[sb]);
-                tc::mma_commit(&a_empty[sa]);
-                if (++kc == kChunk || kb == nkb - 1) {
-                    tc::mma_commit(&acc_full[set]);
-                    kc = 0;
+                const uint64_t b1 = bdesc0 + (uint64_t)((r * bstage) >> 4), b2 = b1 + tile_units;
+                const uint32_t a = a_v + (uint32_t)(128 * (t & 1));
+                tc::mma_ts_f16(d, a, b1, idesc, fresh ? 0u : 1u);
+                tc::mma_ts_f16(d, a + 8, b1 + 2, idesc, 1u);
+                tc::mma_ts_f16(d, a + 16, b1 + 4, idesc, 1u);
+                tc::mma_ts_f16(d, a + 24, b1 + 6, idesc, 1u);
+                tc::mma_ts_f16(d, a + 32, b2, idesc, 1u);
+                tc::mma_ts_f16(d, a + 40, b2 + 2, idesc, 1u);
+                tc::mma_ts_f16(d, a + 48, b2 + 4, idesc, 1u);
+                tc::mma_ts_f16(d, a + 56, b2 + 6, idesc, 1u);
+                tc::mma_commit(&free_[r]);
+                fresh = false;
+                if (--left == 0 || t == nb - 1) {
+                    tc::mma_commit(&acc_full[v]);
                     ++chunk;
+                    left = len;
+                    fresh = true;
                 }
-                if (++sb == SB) sb = 0, bph ^= 1;
-                if (++sa == SA) sa = 0, aph ^= 1;
+                if (++r == R) r = 0, ph ^= 1;
             }
         }
     } else if (warp >= 2 && warp < 2 + 4 * kDecodeGroups) {
@@ -272,29 +299,42 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int q = warp & 3;
         const int r = 32 * q + lane;
         const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
+        const uint32_t a_stage = lane_base + (uint32_t)(a_base + 128 * grp);
         uint32_t G[32], M[32];
-        int sa = grp % SA;
-        uint32_t aph = (uint32_t)(grp / SA) & 1u;
-        for (int kb = grp; kb < nkb; kb += kDecodeGroups) {
-            const int g = kb >> 3, j = kb & 7, sp = g % kPStages;
-            bool ok = tc::mbar_wait(&pk_full[sp], (g / kPStages) & 1, err, 31);
-            ok = ok && tc::mbar_wait(&a_empty[sa], aph ^ 1, err, 32);
+        int ri = grp, fi = grp;  // full ring slot of batch t; free ring slot of batch t - 2
+        uint32_t fph = 0;
+        for (int t = grp; t < nb; t += kDecodeGroups) {
+            const int pg = t >> 2, sp = pg % kPStages;
+            bool ok = tc::mbar_wait(&pk_full[sp], (pg / kPStages) & 1, err, 31);
+            if (t >= kDecodeGroups) {  // this group's A stage was last read by batch t - 2
+                ok = ok && tc::mbar_wait(&free_[fi], fph, err, 32);
+                fi += kDecodeGroups;
+                if (fi >= R) fi -= R, fph ^= 1;
+            }
             if (!__all_sync(0xffffffffu, ok)) break;  // TMEM stores below are warp-collective
             tc::fence_after_sync();
-            const uint4 v = *reinterpret_cast<const uint4 *>(sP + sp * kPStageBytes + r * 128 + ((j ^ (r & 7)) << 4));
-            decode64(v, G, M);
-            tc::tmem_st_x32(lane_base + a_col(sa, 0), G);
-            tc::tmem_st_x32(lane_base + a_col(sa, 1), M);
+            const uint8_t *rowp = sP + sp * kPStageBytes + r * 128;
+            const int j0 = (2 * t) & 7;
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+                const uint4 v = *reinterpret_cast<const uint4 *>(rowp + (((j0 + kk) ^ (r & 7)) << 4));
+                decode64(v, G, M);
+                tc::tmem_st_x32(a_stage + 32 * kk, G);
+                tc::tmem_st_x32(a_stage + 64 + 32 * kk, M);
+            }
             tc::tmem_wait_st();
             tc::fence_before_sync();
-            tc::mbar_arrive(&a_full[sa]);
-            // last K-block of this group inside the packed stage: release the stage
-            if (kb + kDecodeGroups > min(8 * g + 7, nkb - 1)) tc::mbar_arrive(&pk_empty[sp]);
-            sa += kDecodeGroups;  // SA >= kDecodeGroups: one wrap at most
-            if (sa >= SA) sa -= SA, aph ^= 1;
+            __syncwarp();
+            if (lane == 0) {
+                tc::mbar_arrive(&full[ri]);
+                // last batch of this group inside the packed stage: release the stage
+                if (t + kDecodeGroups > min(4 * pg + 3, nb - 1)) tc::mbar_arrive(&pk_empty[sp]);
+            }
+            ri += kDecodeGroups;
+            if (ri >= R) ri -= R;
         }
-    } else if (warp < 14) {
-        // ---------------------------------------------------------- accumulate (warps 10..13)
+    } else if (warp < kIssuerWarpM) {
+        // ---------------------------------------------------------- drain (warps 10..13)
         const int q = warp & 3;
         const int r = 32 * q + lane;
         const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
@@ -306,33 +346,35 @@ __global__ void __launch_bounds__(kThreads, 1)
             a = args.coef[2 * (size_t)row + 1];
         }
         for (int c = 0; c < kParts * kp; ++c) acc[c * 128 + r] = 0;
+        const int nG = chunk_count(nb, kChunkG, kChunkG), nM = chunk_count(nb, kFirstChunkM, kChunkM);
+        int cG = 0, cM = 0;
         bool ok = true;
-        for (int chunk = 0; chunk < nchunks; ++chunk) {
-            const int set = chunk & 1;
-            ok = __all_sync(0xffffffffu, ok && tc::mbar_wait(&acc_full[set], (chunk >> 1) & 1, err, 41, true));
+        // drains in the order the chunks end (G' first on a tie)
+        while (ok && (cG < nG || cM < nM)) {
+            const bool g_next = cG < nG && (cM >= nM || chunk_end(cG, nb, kChunkG, kChunkG) <=
+                                                            chunk_end(cM, nb, kFirstChunkM, kChunkM));
+            const int v = g_next ? 0 : 1;
+            const int c = g_next ? cG++ : cM++;
+            ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[v], c & 1, err, 41, true));
             if (!ok) break;
             tc::fence_after_sync();
-            const uint32_t cb = lane_base + (uint32_t)(set * set_cols);
-            for (int c0 = 0; c0 < kp; c0 += 8) {
-                uint32_t gh[8], gl[8], mh[8], ml[8];
-                tc::tmem_ld_x8(cb + c0, gh);
-                tc::tmem_ld_x8(cb + kp + c0, gl);
-                tc::tmem_ld_x8(cb + N + c0, mh);
-                tc::tmem_ld_x8(cb + N + kp + c0, ml);
-                tc::tmem_wait_ld();
+            // copy the accumulator out (h slices, then l slices), then release it at once
+            const uint32_t cb = lane_base + (uint32_t)(v * N);
+            uint32_t hv[kMaxMixedNrhs], lv[kMaxMixedNrhs];
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                    const long long vg = slices_int(gh[jj], gl[jj]), vm = slices_int(mh[jj], ml[jj]);
-                    if (MODE == kXW) {
-                        acc[(c0 + jj) * 128 + r] += vg;
-                        acc[(kp + c0 + jj) * 128 + r] += vm;
-                    } else {
-                        acc[(c0 + jj) * 128 + r] += vg + vm;
-                    }
+            for (int j = 0; j < kMaxMixedNrhs / 8; ++j)
+                if (8 * j < kp) {
+                    tc::tmem_ld_x8(cb + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(hv + 8 * j));
+                    tc::tmem_ld_x8(cb + kp + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(lv + 8 * j));
                 }
-            }
+            tc::tmem_wait_ld();
             tc::fence_before_sync();
-            tc::mbar_arrive(&acc_empty[set]);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[v]);
+            long long *dst = acc + (MODE == kXW ? v * kp * 128 : 0) + r;
+#pragma unroll
+            for (int j = 0; j < kMaxMixedNrhs; ++j)
+                if (j < kp) dst[j * 128] += slices_int(hv[j], lv[j]);
         }
         const bool valid = ok && row < args.rows;
         const double *sc = args.scales;
@@ -388,38 +430,45 @@ __global__ void __launch_bounds__(256) omega_scales_kernel(const double *__restr
     }
 }
 
-// omega_s[c][i] = h, omega_s[kp + c][i] = l of round(Omega[i][c] * scale_c); zero padding elsewhere.
+// omega_s[c][i] = h, omega_s[kp + c][i] = l of round(Omega[src][c] * scale_c), src = the
+// individual at K position i (perm16 order inside groups of 16); zero padding elsewhere.
 __global__ void __launch_bounds__(256) omega_split_kernel(const double *__restrict__ om, int n, int k, int kp,
                                                           int n_pad, const double *__restrict__ scales,
                                                           __half *__restrict__ out) {
     const int64_t total = (int64_t)kp * n_pad;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int c = (int)(e / n_pad), i = (int)(e - (int64_t)c * n_pad);
+        const int src = (i & ~15) | perm16(i & 15);
         __half hi = __float2half(0.f), lo = __float2half(0.f);
-        if (c < k && i < n) fixed_slices(om[(size_t)i * k + c] * scales[c], hi, lo);
+        if (c < k && src < n) fixed_slices(om[(size_t)src * k + c] * scales[c], hi, lo);
         out[(int64_t)c * n_pad + i] = hi;
         out[(int64_t)(kp + c) * n_pad + i] = lo;
     }
 }
 
 // Scale per column from the exact maxima, then quantise b.Y and a.Y into the X^T Y operand:
-// bop[c] = h(b.Y), bop[kp+c] = l(b.Y), bop[N+c] = h(a.Y), bop[N+kp+c] = l(a.Y).
+// bop[c] = h(b.Y), bop[kp+c] = l(b.Y), bop[N+c] = h(a.Y), bop[N+kp+c] = l(a.Y), at K position s
+// the SNP perm16-ordered inside its group of 16 (zero past the last SNP).
 __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict__ yt, int64_t ld, int n_snp, int k,
                                                         int kp, int N, const double *__restrict__ coef,
                                                         const unsigned int *__restrict__ colmax,
                                                         double *__restrict__ scales, __half *__restrict__ bop) {
-    const int64_t total = (int64_t)k * n_snp;
+    const int n16 = (n_snp + 15) & ~15;
+    const int64_t total = (int64_t)k * n16;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(e / n_snp), s = (int)(e - (int64_t)c * n_snp);
+        const int c = (int)(e / n16), s = (int)(e - (int64_t)c * n16);
+        const int src = (s & ~15) | perm16(s & 15);
         const double sc = pow2_scale_below((double)__uint_as_float(colmax[c]) * 1.001);
         if (s == 0) {
             scales[2 * k + c] = sc;
             scales[3 * k + c] = 1.0 / sc;
         }
-        const double y = (double)yt[(int64_t)c * ld + s] * sc;
-        __half h1, l1, h2, l2;
-        fixed_slices(coef[2 * (size_t)s] * y, h1, l1);
-        fixed_slices(coef[2 * (size_t)s + 1] * y, h2, l2);
+        __half h1 = __float2half(0.f), l1 = h1, h2 = h1, l2 = h1;
+        if (src < n_snp) {
+            const double y = (double)yt[(int64_t)c * ld + src] * sc;
+            fixed_slices(coef[2 * (size_t)src] * y, h1, l1);
+            fixed_slices(coef[2 * (size_t)src + 1] * y, h2, l2);
+        }
         bop[(int64_t)c * ld + s] = h1;
         bop[(int64_t)(kp + c) * ld + s] = l1;
         bop[(int64_t)(N + c) * ld + s] = h2;
@@ -475,24 +524,45 @@ static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base
     return DPCA_OK;
 }
 
+// FP16 slice operand [rows][n_pad] seen as [K-block][rows][64]: one box = one batch of two
+// K-blocks, each a rows x 128 B tile (n_pad is a multiple of 128, so whole batches exist).
+static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, uint64_t rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) {
+        set_error("cuTensorMapEncodeTiled unavailable");
+        return DPCA_ERR_CUDA;
+    }
+    cuuint64_t dims[3] = {64, rows, n_pad / 64};
+    cuuint64_t strides[2] = {n_pad * 2, 128};
+    cuuint32_t box[3] = {64, (cuuint32_t)rows, 2};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (3-D) failed (%d): %llu rows x %llu", (int)r, (unsigned long long)rows,
+                  (unsigned long long)n_pad);
+        return DPCA_ERR_CUDA;
+    }
+    return DPCA_OK;
+}
+
 static MixedState *mstate(Handle *h) { return (MixedState *)h->mx; }
 
 static size_t acc_bytes(int mode, int kp) { return (size_t)(mode == kXW ? 2 : 1) * kp * 128 * 8; }
-
-static size_t smem_bytes(int mode, int N, int kp, int sb, int sa) {
-    size_t b = 1024 + (size_t)kPStages * kPStageBytes + (size_t)sb * (mode == kXW ? 1 : 2) * N * 128 +
-               acc_bytes(mode, kp) + (size_t)(2 * kPStages + 2 * sb + 2 * sa + 4) * 8 + 16;
-    return std::max<size_t>(b, kSmemFloor);
+static size_t batch_bytes(int mode, int N) { return (size_t)2 * (mode == kXW ? 1 : 2) * N * 128; }
+static size_t fixed_bytes(int mode, int kp) {
+    return 1024 + (size_t)kPStages * kPStageBytes + acc_bytes(mode, kp) + 512;  // + barriers
 }
 
-static int pick_sb(int mode, int N, int kp) {
-    const size_t budget = 210 * 1024 - (size_t)kPStages * kPStageBytes - acc_bytes(mode, kp);
-    int sb = (int)(budget / ((size_t)(mode == kXW ? 1 : 2) * N * 128));
-    return std::max(2, std::min(8, sb));
+static int pick_ring(int mode, int N, int kp) {
+    const size_t room = kSmemBudget - fixed_bytes(mode, kp);
+    return std::max(2, std::min(8, (int)(room / batch_bytes(mode, N))));
 }
 
-static int pick_sa(int set_cols) { return std::min(8, (kTmemCols - ((2 * set_cols + 31) & ~31)) / 64); }
-// both products keep one accumulator per MMA issuer: a set is 2 x N columns
+static size_t smem_bytes(int mode, int N, int kp, int ring) {
+    return std::max<size_t>(fixed_bytes(mode, kp) + (size_t)ring * batch_bytes(mode, N), kSmemFloor);
+}
 
 dpca_status mixed_prepare(Handle *h) {
     const int k = h->k;
@@ -506,9 +576,7 @@ dpca_status mixed_prepare(Handle *h) {
         return DPCA_ERR_UNSUPPORTED;
     }
     const int N = m->N;
-    m->sa1 = pick_sa(2 * N);
-    m->sa2 = pick_sa(2 * N);
-    if (m->sa1 < 2 || m->sa2 < 2) {
+    if (((2 * N + 31) & ~31) + 128 * kDecodeGroups > kTmemCols) {
         set_error("internal: TMEM budget exceeded for nrhs %d", k);
         return DPCA_ERR_UNSUPPORTED;
     }
@@ -546,16 +614,14 @@ dpca_status mixed_prepare(Handle *h) {
         set_error("mixed partial allocation: %s", cudaGetErrorString(e));
         return DPCA_ERR_NOMEM;
     }
-    m->sb1 = pick_sb(kXW, N, m->kp);
-    m->sb2 = pick_sb(kXTY, N, m->kp);
-    m->smem1 = smem_bytes(kXW, N, m->kp, m->sb1, m->sa1);
-    m->smem2 = smem_bytes(kXTY, N, m->kp, m->sb2, m->sa2);
+    m->ring1 = pick_ring(kXW, N, m->kp);
+    m->ring2 = pick_ring(kXTY, N, m->kp);
+    m->smem1 = smem_bytes(kXW, N, m->kp, m->ring1);
+    m->smem2 = smem_bytes(kXTY, N, m->kp, m->ring2);
     DPCA_TRY(make_map(&m->map_p, CU_TENSOR_MAP_DATA_TYPE_UINT8, h->P, h->pitch, h->n_snp, h->pitch, 128, 128));
     DPCA_TRY(make_map(&m->map_pt, CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PT, h->pitchT, h->n_ind, h->pitchT, 128, 128));
-    DPCA_TRY(make_map(&m->map_om, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, m->omega_s, h->n_ind_pad, N,
-                      (uint64_t)h->n_ind_pad * 2, 64, N));
-    DPCA_TRY(make_map(&m->map_bop, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, m->bop, h->n_snp_pad, 2 * N,
-                      (uint64_t)h->n_snp_pad * 2, 64, 2 * N));
+    DPCA_TRY(make_batch_map(&m->map_om, m->omega_s, h->n_ind_pad, N));
+    DPCA_TRY(make_batch_map(&m->map_bop, m->bop, h->n_snp_pad, 2 * N));
     DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem1));
     DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)m->smem2));
@@ -592,8 +658,7 @@ dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out) {
     a.k = k;
     a.kp = m->kp;
     a.N = N;
-    a.sa = m->sa1;
-    a.sb = m->sb1;
+    a.ring = m->ring1;
     a.coef = h->coef;
     a.scales = m->scales;
     a.yt = m->yt;
@@ -609,7 +674,7 @@ dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out) {
         DPCA_CUDA(cudaGetLastError());
     }
     ScopedLaunch t(&h->clock, h->stream, "split_bop");
-    int64_t total = (int64_t)k * h->n_snp;
+    int64_t total = (int64_t)k * ((h->n_snp + 15) & ~15);
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 16);
     bop_split_kernel<<<grid, 256, 0, h->stream>>>(m->yt, h->n_snp_pad, h->n_snp, k, m->kp, N, h->coef, m->colmax,
                                                    m->scales, m->bop);
@@ -627,8 +692,7 @@ dpca_status launch_mixed_xty(Handle *h, double *z) {
     a.k = k;
     a.kp = m->kp;
     a.N = N;
-    a.sa = m->sa2;
-    a.sb = m->sb2;
+    a.ring = m->ring2;
     a.scales = m->scales;
     a.partial = m->partial;
     a.err = h->dflag;
