@@ -203,10 +203,14 @@ def dominant(kt: dict, prefer: tuple) -> str:
     return max(cands.items(), key=lambda kv: kv[1]["ms"])[0]
 
 
-def traffic_for(kernel: str):
+def traffic_for(kernel: str, a):
+    """DRAM bytes per launch from the committed ncu summary, if it covers this workload."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             d = json.load(f)
+        w = d.get("workload", {})
+        if (w.get("n_ind"), w.get("n_snp"), w.get("nrhs")) != (a.n_ind, a.n_snp, a.nrhs):
+            return None
         return d.get(kernel)
     except Exception:
         return None
@@ -244,6 +248,7 @@ def dpca_arm(a, ranks: Ranks) -> None:
     e1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
+    h.synchronize()  # raises if a bounded device wait gave up during the timed passes
     ranks.barrier()
     ms = e0.elapsed_time(e1)
     ms_max = ranks.max(ms)
@@ -259,6 +264,12 @@ def dpca_arm(a, ranks: Ranks) -> None:
         roof = {"kernel": dom, "bound": "tensor", "achieved": flops / avg_s / 1e12,
                 "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
                 "peak_source": f"{pk['source']} bf16 sustained (kernel timed inside a multi-pass loop)"}
+        # the exact integer scheme issues two FP16 slices of the dense operand (N = 2 kp) for
+        # each of the G' and M products: 4 x kp / k times the algorithmic MMA work
+        kp = (a.nrhs + 7) // 8 * 8
+        issued = flops * 4 * kp / a.nrhs
+        roof["issued_tensor_flop_per_launch"] = issued
+        roof["frac_issued"] = issued / avg_s / 1e12 / roof["peak"]
     else:
         dom = dominant(kt, ("fp64_xw", "fp64_xty"))
         flops = 2.0 * a.n_snp * a.n_ind * a.nrhs
@@ -266,7 +277,7 @@ def dpca_arm(a, ranks: Ranks) -> None:
         roof = {"kernel": dom, "bound": "fp64", "achieved": flops / avg_s / 1e12, "peak": 1.25, "unit": "TFLOP/s",
                 "peak_source": "nominal FP64 (no measured FP64 peak)"}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = traffic_for(dom)
+    roof["traffic"] = traffic_for(dom, a)
     roof["algorithmic_per_launch"] = f"{flops:.3e} flop (2 x n_snp x n_ind x nrhs)"
     kernels = {k: {"ms_per_launch": v["ms"] / max(1, v["launches"]), "launches": v["launches"],
                    "share": v["ms"] / max(1e-9, sum(x["ms"] for x in kt.values()))} for k, v in kt.items()}

@@ -448,31 +448,39 @@ __global__ void __launch_bounds__(256) omega_split_kernel(const double *__restri
 
 // Scale per column from the exact maxima, then quantise b.Y and a.Y into the X^T Y operand:
 // bop[c] = h(b.Y), bop[kp+c] = l(b.Y), bop[N+c] = h(a.Y), bop[N+kp+c] = l(a.Y), at K position s
-// the SNP perm16-ordered inside its group of 16 (zero past the last SNP).
+// the SNP perm16-ordered inside its group of 16 (zero past the last SNP).  One thread per K
+// position, all columns; the products are formed in FP32 (the scale is a power of two, so the
+// only rounding is the coefficient product's, 2^-24 relative, below the 24-bit quantisation)
+// and split in integer arithmetic: n = 4096 h + l, l in [-2048, 2047], |h| <= 2048.
 __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict__ yt, int64_t ld, int n_snp, int k,
                                                         int kp, int N, const double *__restrict__ coef,
                                                         const unsigned int *__restrict__ colmax,
                                                         double *__restrict__ scales, __half *__restrict__ bop) {
-    const int n16 = (n_snp + 15) & ~15;
-    const int64_t total = (int64_t)k * n16;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(e / n16), s = (int)(e - (int64_t)c * n16);
-        const int src = (s & ~15) | perm16(s & 15);
+    __shared__ float scf[kMaxMixedNrhs];
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
         const double sc = pow2_scale_below((double)__uint_as_float(colmax[c]) * 1.001);
-        if (s == 0) {
+        scf[c] = (float)sc;  // a power of two: exact
+        if (blockIdx.x == 0) {
             scales[2 * k + c] = sc;
             scales[3 * k + c] = 1.0 / sc;
         }
-        __half h1 = __float2half(0.f), l1 = h1, h2 = h1, l2 = h1;
-        if (src < n_snp) {
-            const double y = (double)yt[(int64_t)c * ld + src] * sc;
-            fixed_slices(coef[2 * (size_t)src] * y, h1, l1);
-            fixed_slices(coef[2 * (size_t)src + 1] * y, h2, l2);
+    }
+    __syncthreads();
+    const int n16 = (n_snp + 15) & ~15;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n16; s += gridDim.x * blockDim.x) {
+        const int src = (s & ~15) | perm16(s & 15);
+        const bool valid = src < n_snp;
+        const float b = valid ? (float)coef[2 * (size_t)src] : 0.f;
+        const float a = valid ? (float)coef[2 * (size_t)src + 1] : 0.f;
+        for (int c = 0; c < k; ++c) {
+            const float y = valid ? yt[(int64_t)c * ld + src] * scf[c] : 0.f;
+            const int n1 = __float2int_rn(b * y), n2 = __float2int_rn(a * y);
+            const int h1 = (n1 + 2048) >> 12, h2 = (n2 + 2048) >> 12;
+            bop[(int64_t)c * ld + s] = __int2half_rn(h1);
+            bop[(int64_t)(kp + c) * ld + s] = __int2half_rn(n1 - (h1 << 12));
+            bop[(int64_t)(N + c) * ld + s] = __int2half_rn(h2);
+            bop[(int64_t)(N + kp + c) * ld + s] = __int2half_rn(n2 - (h2 << 12));
         }
-        bop[(int64_t)c * ld + s] = h1;
-        bop[(int64_t)(kp + c) * ld + s] = l1;
-        bop[(int64_t)(N + c) * ld + s] = h2;
-        bop[(int64_t)(N + kp + c) * ld + s] = l2;
     }
 }
 
@@ -674,8 +682,8 @@ dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out) {
         DPCA_CUDA(cudaGetLastError());
     }
     ScopedLaunch t(&h->clock, h->stream, "split_bop");
-    int64_t total = (int64_t)k * ((h->n_snp + 15) & ~15);
-    int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 16);
+    const int n16 = (h->n_snp + 15) & ~15;
+    int grid = std::min(ceil_div(n16, 256), h->sm_count * 8);
     bop_split_kernel<<<grid, 256, 0, h->stream>>>(m->yt, h->n_snp_pad, h->n_snp, k, m->kp, N, h->coef, m->colmax,
                                                    m->scales, m->bop);
     DPCA_CUDA(cudaGetLastError());

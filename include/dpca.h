@@ -76,7 +76,9 @@ typedef struct {
     char prefix[1024]; /* -prefix  output prefix (default "noprefix") */
     int precision;     /* dpca_precision (default DPCA_PREC_MIXED) */
     int device;        /* CUDA device ordinal (default 0) */
-    double hbm_budget_gb; /* packed bytes above this are streamed from pinned host memory (0 = auto) */
+    double hbm_budget_gb; /* reserved for block streaming from pinned host memory, which this version does
+                             not implement: a packed matrix that does not fit the device fails with
+                             DPCA_ERR_NOMEM */
 } dpca_config;
 
 /* Results and the reference's timers (seconds).  sigma and u are caller-owned. */
@@ -86,7 +88,7 @@ typedef struct {
     int total_its;      /* outer iterations performed */
     int passes;         /* applications of X^T X */
     int in_core;        /* 1 when the in-core variant's Gram-form Rayleigh quotient was used */
-    int streamed;       /* 1 when packed blocks were streamed from host memory each pass */
+    int streamed;       /* 1 when packed blocks were streamed from host memory each pass (always 0 here) */
     double *sigma;      /* [nsv]            singular values (sqrt of Ritz values) */
     double *u;          /* [n_ind * nsv]    left singular vectors, row-major */
     double *delta_iter; /* [miter] or NULL  sum of sigma per iteration */
