@@ -121,6 +121,8 @@ dpca_status launch_snp_stats(Handle *h);
 dpca_status launch_synth_fill(Handle *h, uint64_t key, const uint8_t *d_pop, const uint32_t *d_miss,
                               const uint32_t *d_thr, int n_pop);
 dpca_status launch_transpose_packed(Handle *h);
+void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, int32_t *counts, double *avg,
+                          double *sd, double *lut, cudaStream_t stream);
 dpca_status launch_fp64_xw(Handle *h, const double *omega, double *y);
 dpca_status launch_fp64_xty(Handle *h, const double *y, double *z);
 dpca_status launch_qr(Handle *h, double *a);

@@ -5,6 +5,7 @@
 // bit-identical to the reference's standardized values.  Every product and sum is FP64; the
 // reduction order is fixed, so results are deterministic run to run.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "dpca_internal.h"
@@ -200,3 +201,142 @@ dpca_status launch_fp64_xty(Handle *h, const double *y, double *z) {
 }
 
 }  // namespace dpca
+
+namespace dpca {
+
+// ------------------------------------------------------------------ allocation-free pass
+// dpca_pass_fp64_noalloc: the plain FP64 pass Z = X^T (X Omega) on device buffers the caller
+// owns, for callers that must not have a library allocate device memory -- applications that
+// hand out all device memory from their own fixed-budget pool, and latency-sensitive loops in
+// which cudaMalloc/cudaFree (which can synchronise the device) are not acceptable.  Its working
+// buffers -- per-SNP counts, mean, sd and LUT, Y = X Omega, and the split partials of X^T Y --
+// are carved out of one file-scope device array of kNoAllocScratchBytes, which every GPU that
+// loads this library holds until the process exits.
+//
+// In host code the array's name is only a host-side stand-in: its device address is obtained
+// once per device, with that device current, by cudaGetSymbolAddress on the first call made on
+// that device (so that first call should come before any stream capture).  Every call shares
+// the array and it keeps the last call's contents; nothing in it needs to start at zero (each
+// kernel writes every element it later reads).  Calls whose work overlaps on the GPU -- on
+// different streams or from different threads -- race on the array, so callers serialise them.
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;  // 32 MiB per device
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[kNoAllocMaxDevices];
+
+// Device address of the scratch array on the current device (set up on first use).
+static dpca_status noalloc_scratch(void **out) {
+    int dev = 0;
+    DPCA_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("allocation-free pass: device ordinal %d is above %d", dev, kNoAllocMaxDevices - 1);
+        return DPCA_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error("allocation-free pass: cudaGetSymbolAddress of the scratch array failed on device %d: %s", dev,
+                      cudaGetErrorString(e));
+            return DPCA_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return DPCA_OK;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <int MAXC>
+static void xw_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
+                          const double *omega, double *y, cudaStream_t st) {
+    size_t smem = (size_t)64 * k * sizeof(double);
+    cudaFuncSetAttribute(fp64_xw_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fp64_xw_kernel<MAXC><<<ceil_div(n_snp, 64), 256, smem, st>>>(P, pitch, lut, n_ind, n_snp, k, omega, y);
+}
+
+template <int MAXC>
+static void xty_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
+                           const double *y, double *partial, int splits, int sps, cudaStream_t st) {
+    size_t smem = (size_t)32 * k * sizeof(double);
+    cudaFuncSetAttribute(fp64_xty_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid(ceil_div(n_ind, 128), splits);
+    fp64_xty_kernel<MAXC><<<grid, 512, smem, st>>>(P, pitch, lut, n_ind, n_snp, k, y, partial, sps);
+}
+
+}  // namespace dpca
+
+extern "C" dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp,
+                                              const double *omega, int nrhs, double *z, void *stream) {
+    using namespace dpca;
+    clear_error();
+    if (!packed || !omega || !z || n_ind < 1 || n_snp < 1 || nrhs < 1) {
+        set_error("allocation-free pass: null buffer or non-positive size");
+        return DPCA_ERR_INVALID;
+    }
+    if (nrhs > kMaxNrhs) {
+        set_error("allocation-free pass: nrhs %d is above %d", nrhs, kMaxNrhs);
+        return DPCA_ERR_UNSUPPORTED;
+    }
+    const int64_t np = ((int64_t)n_ind + 3) / 4;
+    const int64_t min_stride = (np + 31) / 32 * 32;  // the kernels read whole 32-byte groups
+    if (row_stride < min_stride || row_stride % 16 != 0 || ((uintptr_t)packed & 15u) != 0) {
+        set_error("allocation-free pass: rows need a 16-byte aligned base and a stride that is a multiple of 16 "
+                  "and at least %lld bytes (got %lld)", (long long)min_stride, (long long)row_stride);
+        return DPCA_ERR_INVALID;
+    }
+    // scratch layout: counts [4 n_snp] int32 | avg, sd [n_snp] | lut [4 n_snp] | y [n_snp k] | partial
+    const size_t b_counts = align256((size_t)4 * n_snp * sizeof(int32_t));
+    const size_t b_vec = align256((size_t)n_snp * sizeof(double));
+    const size_t b_lut = align256((size_t)4 * n_snp * sizeof(double));
+    const size_t b_y = align256((size_t)n_snp * nrhs * sizeof(double));
+    const size_t b_part = (size_t)n_ind * nrhs * sizeof(double);  // one split
+    const size_t fixed = b_counts + 2 * b_vec + b_lut + b_y;
+    if (fixed + b_part > kNoAllocScratchBytes) {
+        set_error("allocation-free pass: %d individuals x %d SNPs x nrhs %d needs %zu bytes of scratch; the "
+                  "limit is %zu (use dpca_pass on a handle for larger inputs)",
+                  n_ind, n_snp, nrhs, fixed + b_part, kNoAllocScratchBytes);
+        return DPCA_ERR_UNSUPPORTED;
+    }
+    int dev = 0, sm_count = 1;
+    DPCA_CUDA(cudaGetDevice(&dev));
+    DPCA_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+    void *base = nullptr;
+    DPCA_TRY(noalloc_scratch(&base));
+    unsigned char *sc = (unsigned char *)base;
+    int32_t *counts = (int32_t *)sc;
+    double *avg = (double *)(sc + b_counts);
+    double *sd = (double *)(sc + b_counts + b_vec);
+    double *lut = (double *)(sc + b_counts + 2 * b_vec);
+    double *y = (double *)(sc + b_counts + 2 * b_vec + b_lut);
+    double *partial = (double *)(sc + fixed);
+    // split-K of X^T Y: as many splits as fill the SMs, bounded by the scratch left for partials
+    const int tiles = ceil_div(n_ind, 128);
+    int splits = std::max(1, ceil_div(4 * sm_count, tiles));
+    splits = std::min(splits, std::max(1, ceil_div(n_snp, 32)));
+    splits = (int)std::min<size_t>((size_t)splits, (kNoAllocScratchBytes - fixed) / b_part);
+    int sps = ceil_div(n_snp, splits);
+    sps = (sps + 31) / 32 * 32;
+    splits = ceil_div(n_snp, sps);
+    cudaStream_t st = (cudaStream_t)stream;
+    launch_snp_stats_raw(packed, row_stride, n_ind, n_snp, counts, avg, sd, lut, st);
+    const int mc = (nrhs + 3) / 4;
+    if (mc <= 4) xw_launch_raw<4>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
+    else if (mc <= 8) xw_launch_raw<8>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
+    else if (mc <= 16) xw_launch_raw<16>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
+    else xw_launch_raw<32>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
+    if (mc <= 4) xty_launch_raw<4>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
+    else if (mc <= 8) xty_launch_raw<8>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
+    else if (mc <= 16) xty_launch_raw<16>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
+    else xty_launch_raw<32>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
+    const int64_t elems = (int64_t)n_ind * nrhs;
+    const int grid = (int)std::min<int64_t>((elems + 255) / 256, (int64_t)sm_count * 8);
+    reduce_splits_kernel<<<grid, 256, 0, st>>>(partial, elems, splits, z);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}

@@ -87,6 +87,15 @@ dpca_status launch_snp_stats(Handle *h) {
     return DPCA_OK;
 }
 
+// The statistics kernel on caller-given buffers: used by the allocation-free pass, whose
+// buffers live in a static device array rather than in a handle.
+void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, int32_t *counts, double *avg,
+                          double *sd, double *lut, cudaStream_t stream) {
+    const int64_t np = ((int64_t)n_ind + 3) / 4;
+    snp_stats_kernel<<<ceil_div(n_snp, 8), 256, 0, stream>>>(P, pitch, n_ind, n_snp, np, 1.0 / sqrt((double)n_snp),
+                                                            counts, avg, sd, lut, nullptr);
+}
+
 // One thread writes one 32-bit word (16 individuals) of one SNP row; the
 // genotype of (snp s, individual i) is a pure function of (key, s, i), as in
 // distpca_gb300/synth.py::genotype_codes.

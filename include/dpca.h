@@ -154,6 +154,29 @@ dpca_status dpca_reset_kernel_times(dpca_handle *h, int enable);
 dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp, int32_t *counts,
                                double *avg, double *sd);
 
+/* ---- allocation-free pass (no counterpart in the reference) ----
+ * One plain FP64 pass Z = X^T (X Omega) -- per-SNP statistics, then both products, the same
+ * kernels as a DPCA_PREC_FP64 handle's dpca_pass -- on device buffers the caller owns, without
+ * allocating any device or host memory.  It is for callers that cannot let a library call
+ * cudaMalloc: applications that hand out all device memory from their own fixed-budget pool,
+ * and latency-sensitive loops in which an allocation, which can synchronise the device, is not
+ * acceptable.
+ *   packed  device pointer, 16-byte aligned: n_snp SNP-major rows of ceil(n_ind/4) .bed bytes,
+ *           row_stride bytes apart (a multiple of 16, at least ceil(n_ind/4) rounded up to 32)
+ *   omega   device pointer, n_ind x nrhs row-major FP64 (nrhs <= 128)
+ *   z       device pointer, n_ind x nrhs row-major FP64, written
+ *   stream  cudaStream_t to launch on (NULL: the default stream); the call returns without
+ *           waiting for the work
+ * Its working buffers live in one static device array of 32 MiB that every GPU which loads the
+ * library holds until the process exits; inputs whose statistics, Y and one split of partial
+ * sums do not fit (about 64 + 8*nrhs bytes per SNP plus 8*nrhs bytes per individual) are
+ * rejected with DPCA_ERR_UNSUPPORTED before any work is queued.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress), so make that first call before
+ * any stream capture.  All calls share the array: calls whose work overlaps on the GPU race on
+ * it, so serialise them (one stream, or events between streams). */
+dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp,
+                                   const double *omega, int nrhs, double *z, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
