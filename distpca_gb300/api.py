@@ -79,6 +79,8 @@ _SIGS = {
     "dpca_print_statistics": (None, [ctypes.POINTER(Config), ctypes.POINTER(Result)]),
     "dpca_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "dpca_create_streamed": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "dpca_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dpca_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
     "dpca_synth_fill": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
@@ -233,16 +235,24 @@ def decode_counts(packed: np.ndarray, n_ind: int):
 
 
 class Handle:
-    """A genotype matrix resident on one GPU plus the subspace state."""
+    """A genotype matrix on one GPU plus the subspace state.
+
+    block_snps > 0 makes a streaming handle: the rows stay in host memory (the array given to
+    upload, kept referenced here) and every pass copies them in blocks of block_snps SNPs.
+    """
 
     def __init__(self, n_ind: int, n_snp: int, nrhs: int, precision=PREC_MIXED, device: int = 0,
-                 stream: Optional[int] = None):
+                 stream: Optional[int] = None, block_snps: int = 0):
         if isinstance(precision, str):
             precision = {"fp64": PREC_FP64, "mixed": PREC_MIXED}[precision]
         self.n_ind, self.n_snp, self.nrhs, self.precision = n_ind, n_snp, nrhs, precision
+        self._host = None
         h = ctypes.c_void_p()
-        _check(lib().dpca_create(ctypes.byref(h), n_ind, n_snp, nrhs, precision, device,
-                                 ctypes.c_void_p(stream) if stream else None))
+        st = ctypes.c_void_p(stream) if stream else None
+        if block_snps > 0:
+            _check(lib().dpca_create_streamed(ctypes.byref(h), n_ind, n_snp, nrhs, precision, device, st, block_snps))
+        else:
+            _check(lib().dpca_create(ctypes.byref(h), n_ind, n_snp, nrhs, precision, device, st))
         self._h = h
 
     def close(self) -> None:
@@ -265,6 +275,7 @@ class Handle:
     def upload(self, packed: np.ndarray) -> None:
         packed = np.ascontiguousarray(packed, dtype=np.uint8)
         assert packed.shape[0] == self.n_snp
+        self._host = packed  # a streaming handle reads these rows in every pass
         _check(lib().dpca_upload(self._h, _p(packed), packed.shape[1]))
 
     def upload_ptr(self, ptr: int, row_stride: int) -> None:

@@ -99,6 +99,19 @@ struct Handle {
     // mixed-precision operands
     void *mx = nullptr;         // MixedState (k_mixed.cu)
 
+    // Streaming (the packed matrix stays in host memory and is copied in blocks each pass).
+    // Device buffers then hold `rows_dev` = blk SNP rows instead of n_snp.
+    bool streamed = false;
+    int blk = 0, nblk = 0;            // SNP rows per block (multiple of 128), number of blocks
+    int rows_dev = 0;                 // SNP rows resident at a time: n_snp, or blk when streamed
+    const uint8_t *hostP = nullptr;   // caller-owned host rows, host_stride bytes apart
+    int64_t host_stride = 0;
+    uint8_t *Pb[2] = {nullptr, nullptr};   // block buffers, blk x pitch
+    uint8_t *PTb[2] = {nullptr, nullptr};  // mixed: block transposes, n_ind x pitchTb
+    int64_t pitchTb = 0;
+    cudaStream_t cstream = nullptr;        // copy stream
+    cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+
     KernelClock clock;
 };
 
@@ -121,8 +134,14 @@ dpca_status launch_snp_stats(Handle *h);
 dpca_status launch_synth_fill(Handle *h, uint64_t key, const uint8_t *d_pop, const uint32_t *d_miss,
                               const uint32_t *d_thr, int n_pop);
 dpca_status launch_transpose_packed(Handle *h);
-void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, int32_t *counts, double *avg,
-                          double *sd, double *lut, cudaStream_t stream);
+void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, double inv_sqrt_nsnp,
+                          int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream);
+void launch_transpose_raw(const uint8_t *P, int64_t pitch, uint8_t *PT, int64_t pitchT, int n_ind, int n_snp,
+                          cudaStream_t stream);
+// one streamed block: Z (+)= X_b^T (X_b Omega) over SNP rows [s0, s0 + ns) held in buffer b
+dpca_status launch_fp64_block(Handle *h, int b, int s0, int ns, const double *omega, double *z, bool accumulate);
+dpca_status mixed_omega_operand(Handle *h, const double *omega);
+dpca_status mixed_block(Handle *h, int b, int s0, int ns, double *z, bool accumulate);
 dpca_status launch_fp64_xw(Handle *h, const double *omega, double *y);
 dpca_status launch_fp64_xty(Handle *h, const double *y, double *z);
 dpca_status launch_qr(Handle *h, double *a);

@@ -98,15 +98,22 @@ static dpca_status dalloc(T **p, size_t elems) {
 
 static void free_all(Handle *h) {
     if (h->mx) mixed_release(h);
-    void *ptrs[] = {h->P, h->PT, h->counts, h->avg, h->sd, h->lut, h->coef, h->omega, h->z, h->q,
-                    h->old, h->work, h->y, h->partial, h->small, h->red, h->dflag};
+    void *ptrs[] = {h->P,     h->PT,    h->counts, h->avg,      h->sd,  h->lut,    h->coef,
+                    h->omega, h->z,     h->q,      h->old,      h->work, h->y,     h->partial,
+                    h->small, h->red,   h->dflag,  h->Pb[0],    h->Pb[1], h->PTb[0], h->PTb[1]};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (int b = 0; b < 2; ++b) {
+        if (h->copied[b]) cudaEventDestroy(h->copied[b]);
+        if (h->consumed[b]) cudaEventDestroy(h->consumed[b]);
+    }
+    if (h->cstream) cudaStreamDestroy(h->cstream);
     if (h->host_small) cudaFreeHost(h->host_small);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
-static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int precision, int device, void *stream) {
+static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int precision, int device, void *stream,
+                               int block_snps) {
     if (n_ind <= 0 || n_snp <= 0 || nrhs <= 0) {
         set_error("dpca_create: n_ind, n_snp and nrhs must be positive");
         return DPCA_ERR_INVALID;
@@ -151,8 +158,29 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
     h->n_snp_pad = (int)round_up((size_t)n_snp, 128);
     h->inv_sqrt_nsnp = 1.0 / sqrt((double)n_snp);
     size_t nk = (size_t)n_ind * nrhs;
-    DPCA_TRY(dalloc(&h->P, (size_t)n_snp * h->pitch));
-    DPCA_CUDA(cudaMemsetAsync(h->P, 0, (size_t)n_snp * h->pitch, h->stream));
+    h->streamed = block_snps > 0 && block_snps < n_snp;
+    h->rows_dev = n_snp;
+    if (h->streamed) {
+        // two block buffers (double buffering) instead of the whole matrix
+        h->blk = (int)std::min<size_t>(round_up((size_t)block_snps, 128), (size_t)n_snp);
+        h->nblk = (n_snp + h->blk - 1) / h->blk;
+        h->rows_dev = h->blk;
+        h->pitchTb = (int64_t)round_up((size_t)(h->blk + 3) / 4, 128);
+        for (int b = 0; b < 2; ++b) {
+            DPCA_TRY(dalloc(&h->Pb[b], (size_t)h->blk * h->pitch));
+            DPCA_CUDA(cudaMemsetAsync(h->Pb[b], 0, (size_t)h->blk * h->pitch, h->stream));
+            if (precision == DPCA_PREC_MIXED) {
+                DPCA_TRY(dalloc(&h->PTb[b], (size_t)n_ind * h->pitchTb));
+                DPCA_CUDA(cudaMemsetAsync(h->PTb[b], 0, (size_t)n_ind * h->pitchTb, h->stream));
+            }
+            DPCA_CUDA(cudaEventCreateWithFlags(&h->copied[b], cudaEventDisableTiming));
+            DPCA_CUDA(cudaEventCreateWithFlags(&h->consumed[b], cudaEventDisableTiming));
+        }
+        DPCA_CUDA(cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking));
+    } else {
+        DPCA_TRY(dalloc(&h->P, (size_t)n_snp * h->pitch));
+        DPCA_CUDA(cudaMemsetAsync(h->P, 0, (size_t)n_snp * h->pitch, h->stream));
+    }
     DPCA_TRY(dalloc(&h->counts, 4 * (size_t)n_snp));
     DPCA_TRY(dalloc(&h->avg, (size_t)n_snp));
     DPCA_TRY(dalloc(&h->sd, (size_t)n_snp));
@@ -163,12 +191,12 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
     DPCA_TRY(dalloc(&h->q, nk));
     DPCA_TRY(dalloc(&h->old, nk));
     DPCA_TRY(dalloc(&h->work, nk));
-    DPCA_TRY(dalloc(&h->y, (size_t)n_snp * nrhs));
+    DPCA_TRY(dalloc(&h->y, (size_t)h->rows_dev * nrhs));
     // FP64 split-K partials: up to ceil(4*SMs / tiles) splits
     {
         int tiles = (n_ind + 127) / 128;
         int s = std::max(1, (4 * h->sm_count + tiles - 1) / tiles);
-        s = std::min(s, std::max(1, (n_snp + 31) / 32));
+        s = std::min(s, std::max(1, (h->rows_dev + 31) / 32));
         h->partial_elems = (size_t)s * nk;
         DPCA_TRY(dalloc(&h->partial, h->partial_elems));
     }
@@ -182,15 +210,64 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
     DPCA_CUDA(cudaMemsetAsync(h->dflag, 0, 16 * sizeof(int), h->stream));
     DPCA_CUDA(cudaMallocHost((void **)&h->host_small, L.total() * sizeof(double)));
     if (precision == DPCA_PREC_MIXED) {
-        DPCA_TRY(dalloc(&h->PT, (size_t)n_ind * h->pitchT));
-        DPCA_CUDA(cudaMemsetAsync(h->PT, 0, (size_t)n_ind * h->pitchT, h->stream));
+        if (!h->streamed) {
+            DPCA_TRY(dalloc(&h->PT, (size_t)n_ind * h->pitchT));
+            DPCA_CUDA(cudaMemsetAsync(h->PT, 0, (size_t)n_ind * h->pitchT, h->stream));
+        }
         DPCA_TRY(mixed_prepare(h));
     }
     h->clock.enabled = env_flag("DPCA_KERNEL_CLOCK");
     return DPCA_OK;
 }
 
+// Streaming: copy block j of the host rows into buffer j % 2 on the copy stream, after the
+// compute stream has finished with the block that used that buffer last, and make the compute
+// stream wait for the copy.
+static dpca_status stream_in(Handle *h, int j, int *s0, int *ns) {
+    const int b = j & 1;
+    *s0 = j * h->blk;
+    *ns = std::min(h->blk, h->n_snp - *s0);
+    DPCA_CUDA(cudaStreamWaitEvent(h->cstream, h->consumed[b], 0));
+    DPCA_CUDA(cudaMemcpy2DAsync(h->Pb[b], h->pitch, h->hostP + (int64_t)*s0 * h->host_stride, h->host_stride, h->np,
+                                *ns, cudaMemcpyHostToDevice, h->cstream));
+    DPCA_CUDA(cudaEventRecord(h->copied[b], h->cstream));
+    DPCA_CUDA(cudaStreamWaitEvent(h->stream, h->copied[b], 0));
+    return DPCA_OK;
+}
+
+// Per-SNP statistics of a streamed matrix: one sweep over the blocks.
+static dpca_status streamed_stats(Handle *h) {
+    for (int j = 0; j < h->nblk; ++j) {
+        int s0 = 0, ns = 0;
+        DPCA_TRY(stream_in(h, j, &s0, &ns));
+        {
+            ScopedLaunch t(&h->clock, h->stream, "snp_stats");
+            launch_snp_stats_raw(h->Pb[j & 1], h->pitch, h->n_ind, ns, h->inv_sqrt_nsnp, h->counts + 4 * (size_t)s0,
+                                 h->avg + s0, h->sd + s0, h->lut + 4 * (size_t)s0, h->coef + 2 * (size_t)s0,
+                                 h->stream);
+            DPCA_CUDA(cudaGetLastError());
+        }
+        DPCA_CUDA(cudaEventRecord(h->consumed[j & 1], h->stream));
+    }
+    h->stats_ready = true;
+    return DPCA_OK;
+}
+
+// One pass over a streamed matrix: blocks arrive double-buffered; Z accumulates over them.
+static dpca_status streamed_pass(Handle *h, const double *in, double *out) {
+    if (h->precision == DPCA_PREC_MIXED) DPCA_TRY(mixed_omega_operand(h, in));
+    for (int j = 0; j < h->nblk; ++j) {
+        int s0 = 0, ns = 0;
+        DPCA_TRY(stream_in(h, j, &s0, &ns));
+        if (h->precision == DPCA_PREC_FP64) DPCA_TRY(launch_fp64_block(h, j & 1, s0, ns, in, out, j > 0));
+        else DPCA_TRY(mixed_block(h, j & 1, s0, ns, out, j > 0));
+        DPCA_CUDA(cudaEventRecord(h->consumed[j & 1], h->stream));
+    }
+    return DPCA_OK;
+}
+
 static dpca_status after_data(Handle *h) {
+    if (h->streamed) return streamed_stats(h);
     DPCA_TRY(launch_snp_stats(h));
     if (h->precision == DPCA_PREC_MIXED) {
         DPCA_TRY(launch_transpose_packed(h));
@@ -204,6 +281,7 @@ dpca_status handle_pass_io(Handle *h, const double *in, double *out) {
         set_error("no genotype data on the device (call dpca_upload or dpca_synth_fill)");
         return DPCA_ERR_INVALID;
     }
+    if (h->streamed) return streamed_pass(h, in, out);
     if (h->precision == DPCA_PREC_FP64) {
         DPCA_TRY(launch_fp64_xw(h, in, h->y));
         DPCA_TRY(launch_fp64_xty(h, h->y, out));
@@ -255,7 +333,8 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
         set_error("no genotype data on the device");
         return DPCA_ERR_INVALID;
     }
-    const bool in_core = cfg->bsize >= h->n_snp;
+    // the in-core variant's Gram form needs Y = X Q of every SNP at once: resident matrices only
+    const bool in_core = cfg->bsize >= h->n_snp && !h->streamed;
     const size_t nkb = (size_t)n * k * sizeof(double);
     SmallLayout L{k};
     bool clock_was = h->clock.enabled;
@@ -333,6 +412,7 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     res->total_its = stopped ? ii + 1 : ii;
     res->passes = passes;
     res->in_core = in_core ? 1 : 0;
+    res->streamed = h->streamed ? 1 : 0;
     if (res->sigma) memcpy(res->sigma, h->host_small + L.sigma(), (size_t)nsv * sizeof(double));
     if (res->u)
         for (int i = 0; i < n; ++i)
@@ -370,7 +450,28 @@ dpca_status dpca_create(dpca_handle **out, int n_ind, int n_snp, int nrhs, int p
     *out = nullptr;
     dpca_handle *hh = new (std::nothrow) dpca_handle();
     if (!hh) return DPCA_ERR_NOMEM;
-    dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream);
+    dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream, 0);
+    if (st != DPCA_OK) {
+        free_all(&hh->h);
+        delete hh;
+        return st;
+    }
+    *out = hh;
+    return DPCA_OK;
+}
+
+dpca_status dpca_create_streamed(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device,
+                                 void *stream, int block_snps) {
+    clear_error();
+    if (!out) return DPCA_ERR_INVALID;
+    *out = nullptr;
+    if (block_snps <= 0) {
+        set_error("dpca_create_streamed: block_snps must be positive");
+        return DPCA_ERR_INVALID;
+    }
+    dpca_handle *hh = new (std::nothrow) dpca_handle();
+    if (!hh) return DPCA_ERR_NOMEM;
+    dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream, block_snps);
     if (st != DPCA_OK) {
         free_all(&hh->h);
         delete hh;
@@ -398,6 +499,13 @@ dpca_status dpca_upload(dpca_handle *hh, const uint8_t *packed, int64_t row_stri
         return DPCA_ERR_INVALID;
     }
     DPCA_CUDA(cudaSetDevice(h->device));
+    if (h->streamed) {
+        // the rows stay in host memory and are read block by block in every pass
+        h->hostP = packed;
+        h->host_stride = row_stride;
+        DPCA_TRY(after_data(h));
+        return DPCA_OK;
+    }
     {
         ScopedLaunch t(&h->clock, h->stream, "h2d_packed");
         // chunked 2D copies keep each transfer bounded
@@ -417,6 +525,10 @@ dpca_status dpca_synth_fill(dpca_handle *hh, uint64_t key, const uint8_t *pop, c
     clear_error();
     if (!hh || !pop || !miss_thr || !snp_thr || n_pop <= 0) return DPCA_ERR_INVALID;
     Handle *h = &hh->h;
+    if (h->streamed) {
+        set_error("dpca_synth_fill: a streaming handle reads its rows from host memory (use dpca_upload)");
+        return DPCA_ERR_UNSUPPORTED;
+    }
     DPCA_CUDA(cudaSetDevice(h->device));
     uint8_t *d_pop = nullptr;
     uint32_t *d_miss = nullptr, *d_thr = nullptr;
@@ -445,6 +557,14 @@ dpca_status dpca_download_packed(dpca_handle *hh, int s0, int s1, uint8_t *out) 
         return DPCA_ERR_INVALID;
     }
     DPCA_CUDA(cudaSetDevice(h->device));
+    if (h->streamed) {
+        if (!h->hostP) {
+            set_error("no genotype rows attached (call dpca_upload)");
+            return DPCA_ERR_INVALID;
+        }
+        for (int s = s0; s < s1; ++s) memcpy(out + (size_t)(s - s0) * h->np, h->hostP + (int64_t)s * h->host_stride, h->np);
+        return DPCA_OK;
+    }
     if (s1 > s0)
         DPCA_CUDA(cudaMemcpy2DAsync(out, h->np, h->P + (int64_t)s0 * h->pitch, h->pitch, h->np, s1 - s0,
                                     cudaMemcpyDeviceToHost, h->stream));

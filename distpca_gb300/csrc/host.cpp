@@ -128,13 +128,37 @@ static dpca_status run_common(const dpca_config *cfg_in, const char *bfile, cons
     cfg.bsize = rows;
     res->rows_fetched = rows;
     double t0 = wall_now();
+    // Resident or streamed: the packed matrix (twice on the mixed path, which also keeps its
+    // individual-major transpose) must fit the device budget -- -hbm GB, else 85% of the free
+    // device memory -- or it is streamed from host memory in blocks of at most 2 GB, two in
+    // flight.
+    const int64_t np = (n_ind + 3) / 4;
+    const size_t pitch = ((size_t)np + 127) / 128 * 128;
+    const size_t per_row = pitch * (cfg.precision == DPCA_PREC_MIXED ? 2 : 1);
+    size_t budget = 0;
+    if (cfg.hbm_budget_gb > 0) {
+        budget = (size_t)(cfg.hbm_budget_gb * 1e9);
+    } else {
+        size_t fr = 0, tot = 0;
+        if (cudaSetDevice(cfg.device) == cudaSuccess && cudaMemGetInfo(&fr, &tot) == cudaSuccess)
+            budget = (size_t)(0.85 * (double)fr);
+        else
+            cudaGetLastError();
+    }
+    int block_snps = 0;
+    if (budget > 0 && per_row * (size_t)n_snp > budget) {
+        size_t rows = std::min<size_t>((size_t)2000000000 / pitch, budget / (2 * per_row));
+        block_snps = (int)std::max<size_t>(128, rows / 128 * 128);
+    }
     dpca_handle *hh = nullptr;
-    DPCA_TRY(dpca_create(&hh, n_ind, n_snp, cfg.nrhs, cfg.precision, cfg.device, nullptr));
+    if (block_snps > 0 && block_snps < n_snp)
+        DPCA_TRY(dpca_create_streamed(&hh, n_ind, n_snp, cfg.nrhs, cfg.precision, cfg.device, nullptr, block_snps));
+    else
+        DPCA_TRY(dpca_create(&hh, n_ind, n_snp, cfg.nrhs, cfg.precision, cfg.device, nullptr));
     std::vector<uint8_t> filebuf;
     uint8_t *pinned = nullptr;
     const uint8_t *src = packed_host;
     int64_t stride = row_stride;
-    int64_t np = (n_ind + 3) / 4;
     dpca_status st = DPCA_OK;
     if (!src) {
         // the whole .bed payload, in pinned memory when the host allows it

@@ -127,13 +127,14 @@ __global__ void __launch_bounds__(512) fp64_xty_kernel(const uint8_t *__restrict
     }
 }
 
-// z[e] = sum over splits of partial[split][e], in split order.
+// z[e] = sum over splits of partial[split][e], in split order (added to z when accumulating,
+// as the streamed blocks do).
 __global__ void reduce_splits_kernel(const double *__restrict__ partial, int64_t elems, int splits,
-                                     double *__restrict__ z) {
+                                     double *__restrict__ z, int accumulate = 0) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < elems; e += (int64_t)gridDim.x * blockDim.x) {
         double s = 0.0;
         for (int p = 0; p < splits; ++p) s += partial[(int64_t)p * elems + e];
-        z[e] = s;
+        z[e] = accumulate ? z[e] + s : s;
     }
 }
 
@@ -269,6 +270,43 @@ static void xty_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, i
     fp64_xty_kernel<MAXC><<<grid, 512, smem, st>>>(P, pitch, lut, n_ind, n_snp, k, y, partial, sps);
 }
 
+// One streamed block of the FP64 pass: Y_b = X_b Omega into h->y (blk x k), then
+// z (+)= X_b^T Y_b through split partials, rows [s0, s0 + ns) of the matrix in buffer Pb[b].
+dpca_status launch_fp64_block(Handle *h, int b, int s0, int ns, const double *omega, double *z, bool accumulate) {
+    const uint8_t *P = h->Pb[b];
+    const double *lut = h->lut + 4 * (size_t)s0;
+    const int k = h->k, mc = (k + 3) / 4;
+    {
+        ScopedLaunch t(&h->clock, h->stream, "fp64_xw");
+        if (mc <= 4) xw_launch_raw<4>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
+        else if (mc <= 8) xw_launch_raw<8>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
+        else if (mc <= 16) xw_launch_raw<16>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
+        else xw_launch_raw<32>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    const int tiles = ceil_div(h->n_ind, 128);
+    int splits = std::max(1, ceil_div(4 * h->sm_count, tiles));
+    splits = std::min(splits, std::max(1, ceil_div(ns, 32)));
+    splits = (int)std::max<int64_t>(1, std::min<int64_t>(splits, (int64_t)(h->partial_elems / ((size_t)h->n_ind * k))));
+    int sps = ceil_div(ns, splits);
+    sps = (sps + 31) / 32 * 32;
+    splits = ceil_div(ns, sps);
+    {
+        ScopedLaunch t(&h->clock, h->stream, "fp64_xty");
+        if (mc <= 4) xty_launch_raw<4>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
+        else if (mc <= 8) xty_launch_raw<8>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
+        else if (mc <= 16) xty_launch_raw<16>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
+        else xty_launch_raw<32>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    ScopedLaunch t(&h->clock, h->stream, "reduce_splits");
+    const int64_t elems = (int64_t)h->n_ind * k;
+    const int grid = (int)std::min<int64_t>((elems + 255) / 256, (int64_t)h->sm_count * 8);
+    reduce_splits_kernel<<<grid, 256, 0, h->stream>>>(h->partial, elems, splits, z, accumulate ? 1 : 0);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
 }  // namespace dpca
 
 extern "C" dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp,
@@ -324,7 +362,8 @@ extern "C" dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row
     sps = (sps + 31) / 32 * 32;
     splits = ceil_div(n_snp, sps);
     cudaStream_t st = (cudaStream_t)stream;
-    launch_snp_stats_raw(packed, row_stride, n_ind, n_snp, counts, avg, sd, lut, st);
+    launch_snp_stats_raw(packed, row_stride, n_ind, n_snp, 1.0 / sqrt((double)n_snp), counts, avg, sd, lut, nullptr,
+                         st);
     const int mc = (nrhs + 3) / 4;
     if (mc <= 4) xw_launch_raw<4>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
     else if (mc <= 8) xw_launch_raw<8>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);

@@ -102,7 +102,8 @@ struct MixedState {
     int splits = 1, kb_per_split = 8;
     int ring1 = 2, ring2 = 2;
     size_t smem1 = 0, smem2 = 0;
-    CUtensorMap map_p, map_pt, map_om, map_bop;
+    int splits_cap = 1;          // partial buffer capacity (splits)
+    CUtensorMap map_p[2], map_pt[2], map_om, map_bop;  // [1]: second block buffer when streaming
 };
 
 // ------------------------------------------------------------------ decode
@@ -466,8 +467,10 @@ __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict_
         }
     }
     __syncthreads();
-    const int n16 = (n_snp + 15) & ~15;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n16; s += gridDim.x * blockDim.x) {
+    // K positions up to the next whole batch (128 SNPs) are written, zeros past the last SNP, so
+    // that a reused (streamed) operand buffer holds no stale values inside the K range
+    const int n128 = (n_snp + 127) & ~127;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n128; s += gridDim.x * blockDim.x) {
         const int src = (s & ~15) | perm16(s & 15);
         const bool valid = src < n_snp;
         const float b = valid ? (float)coef[2 * (size_t)src] : 0.f;
@@ -485,11 +488,11 @@ __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict_
 }
 
 __global__ void reduce_parts_kernel(const double *__restrict__ partial, int64_t elems, int splits,
-                                    double *__restrict__ z) {
+                                    double *__restrict__ z, int accumulate) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < elems; e += (int64_t)gridDim.x * blockDim.x) {
         double s = 0.0;
         for (int p = 0; p < splits; ++p) s += partial[(int64_t)p * elems + e];
-        z[e] = s;
+        z[e] = accumulate ? z[e] + s : s;
     }
 }
 
@@ -572,6 +575,27 @@ static size_t smem_bytes(int mode, int N, int kp, int ring) {
     return std::max<size_t>(fixed_bytes(mode, kp) + (size_t)ring * batch_bytes(mode, N), kSmemFloor);
 }
 
+// Split-K of X^T Y over nsnp SNPs: fill the SMs evenly (one CTA per SM owns all of TMEM).
+static void pick_splits(const Handle *h, int nsnp, int *kb_per_split, int *splits) {
+    const int tiles2 = ceil_div(h->n_ind, 128);
+    const int nkb2 = ceil_div(nsnp, 64);
+    const int ngroups = ceil_div(nkb2, 8);
+    double best = -1.0;
+    int best_s = 1;
+    for (int s = 1; s <= std::min(16, ngroups); ++s) {
+        int per = ceil_div(ngroups, s);
+        int sreal = ceil_div(ngroups, per);
+        int64_t items = (int64_t)tiles2 * sreal;
+        double eff = (double)items / (double)(h->sm_count * ((items + h->sm_count - 1) / h->sm_count));
+        if (eff > best + 0.02) {
+            best = eff;
+            best_s = sreal;
+        }
+    }
+    *kb_per_split = 8 * ceil_div(ngroups, best_s);
+    *splits = ceil_div(nkb2, *kb_per_split);
+}
+
 dpca_status mixed_prepare(Handle *h) {
     const int k = h->k;
     MixedState *m = new (std::nothrow) MixedState();
@@ -588,37 +612,24 @@ dpca_status mixed_prepare(Handle *h) {
         set_error("internal: TMEM budget exceeded for nrhs %d", k);
         return DPCA_ERR_UNSUPPORTED;
     }
+    // SNP-indexed operands cover the rows resident at a time (all SNPs, or one streamed block)
+    const int rows_pad = (h->rows_dev + 127) / 128 * 128;
     cudaError_t e;
-    size_t om_elems = (size_t)N * h->n_ind_pad, bop_elems = (size_t)2 * N * h->n_snp_pad;
+    size_t om_elems = (size_t)N * h->n_ind_pad, bop_elems = (size_t)2 * N * rows_pad;
     if ((e = cudaMalloc(&m->omega_s, om_elems * 2)) != cudaSuccess ||
         (e = cudaMalloc(&m->bop, bop_elems * 2)) != cudaSuccess ||
         (e = cudaMalloc(&m->scales, 4 * (size_t)k * 8)) != cudaSuccess ||
-        (e = cudaMalloc(&m->yt, (size_t)k * h->n_snp_pad * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&m->yt, (size_t)k * rows_pad * 4)) != cudaSuccess ||
         (e = cudaMalloc(&m->colmax, (size_t)k * 4)) != cudaSuccess) {
         set_error("mixed operand allocation: %s", cudaGetErrorString(e));
         return DPCA_ERR_NOMEM;
     }
     DPCA_CUDA(cudaMemsetAsync(m->omega_s, 0, om_elems * 2, h->stream));
     DPCA_CUDA(cudaMemsetAsync(m->bop, 0, bop_elems * 2, h->stream));
-    // split-K of X^T Y over SNPs: fill the SMs evenly (one CTA per SM owns all of TMEM)
-    const int tiles2 = ceil_div(h->n_ind, 128);
-    const int nkb2 = ceil_div(h->n_snp, 64);
-    const int ngroups = ceil_div(nkb2, 8);
-    double best = -1.0;
-    int best_s = 1;
-    for (int s = 1; s <= std::min(16, ngroups); ++s) {
-        int per = ceil_div(ngroups, s);
-        int sreal = ceil_div(ngroups, per);
-        int64_t items = (int64_t)tiles2 * sreal;
-        double eff = (double)items / (double)(h->sm_count * ((items + h->sm_count - 1) / h->sm_count));
-        if (eff > best + 0.02) {
-            best = eff;
-            best_s = sreal;
-        }
-    }
-    m->kb_per_split = 8 * ceil_div(ngroups, best_s);
-    m->splits = ceil_div(nkb2, m->kb_per_split);
-    if ((e = cudaMalloc(&m->partial, (size_t)m->splits * h->n_ind * k * 8)) != cudaSuccess) {
+    pick_splits(h, h->rows_dev, &m->kb_per_split, &m->splits);
+    // a shorter (last) streamed block may pick more splits: room for the most the rule allows
+    m->splits_cap = h->streamed ? 16 : m->splits;
+    if ((e = cudaMalloc(&m->partial, (size_t)m->splits_cap * h->n_ind * k * 8)) != cudaSuccess) {
         set_error("mixed partial allocation: %s", cudaGetErrorString(e));
         return DPCA_ERR_NOMEM;
     }
@@ -626,10 +637,20 @@ dpca_status mixed_prepare(Handle *h) {
     m->ring2 = pick_ring(kXTY, N, m->kp);
     m->smem1 = smem_bytes(kXW, N, m->kp, m->ring1);
     m->smem2 = smem_bytes(kXTY, N, m->kp, m->ring2);
-    DPCA_TRY(make_map(&m->map_p, CU_TENSOR_MAP_DATA_TYPE_UINT8, h->P, h->pitch, h->n_snp, h->pitch, 128, 128));
-    DPCA_TRY(make_map(&m->map_pt, CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PT, h->pitchT, h->n_ind, h->pitchT, 128, 128));
+    if (!h->streamed) {
+        DPCA_TRY(make_map(&m->map_p[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->P, h->pitch, h->n_snp, h->pitch, 128, 128));
+        DPCA_TRY(make_map(&m->map_pt[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PT, h->pitchT, h->n_ind, h->pitchT, 128,
+                          128));
+    } else {
+        for (int b = 0; b < 2; ++b) {
+            DPCA_TRY(make_map(&m->map_p[b], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->Pb[b], h->pitch, h->blk, h->pitch, 128,
+                              128));
+            DPCA_TRY(make_map(&m->map_pt[b], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PTb[b], h->pitchTb, h->n_ind,
+                              h->pitchTb, 128, 128));
+        }
+    }
     DPCA_TRY(make_batch_map(&m->map_om, m->omega_s, h->n_ind_pad, N));
-    DPCA_TRY(make_batch_map(&m->map_bop, m->bop, h->n_snp_pad, 2 * N));
+    DPCA_TRY(make_batch_map(&m->map_bop, m->bop, rows_pad, 2 * N));
     DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem1));
     DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)m->smem2));
@@ -647,75 +668,107 @@ dpca_status mixed_release(Handle *h) {
     return DPCA_OK;
 }
 
-dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out) {
+// Quantise Omega into its two FP16 slices (once per pass, shared by every block).
+dpca_status mixed_omega_operand(Handle *h, const double *omega) {
+    MixedState *m = mstate(h);
+    const int k = h->k;
+    ScopedLaunch t(&h->clock, h->stream, "split_omega");
+    omega_scales_kernel<<<k, 256, 0, h->stream>>>(omega, h->n_ind, k, m->scales);
+    int64_t total = (int64_t)m->kp * h->n_ind_pad;
+    int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 8);
+    omega_split_kernel<<<grid, 256, 0, h->stream>>>(omega, h->n_ind, k, m->kp, h->n_ind_pad, m->scales, m->omega_s);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
+// Y = X Omega for `rows` SNP rows behind map_a (coefficients from coef), then the X^T Y operand.
+static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const double *coef, double *y_out) {
     MixedState *m = mstate(h);
     const int k = h->k, N = m->N;
-    {
-        ScopedLaunch t(&h->clock, h->stream, "split_omega");
-        omega_scales_kernel<<<k, 256, 0, h->stream>>>(omega, h->n_ind, k, m->scales);
-        int64_t total = (int64_t)m->kp * h->n_ind_pad;
-        int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 8);
-        omega_split_kernel<<<grid, 256, 0, h->stream>>>(omega, h->n_ind, k, m->kp, h->n_ind_pad, m->scales,
-                                                        m->omega_s);
-        DPCA_CUDA(cudaGetLastError());
-    }
+    const int rows_pad = (h->rows_dev + 127) / 128 * 128;
     GemmArgs a{};
-    a.rows = h->n_snp;
+    a.rows = rows;
     a.nkb_total = ceil_div(h->n_ind, 64);
     a.kb_per_split = 8 * ceil_div(a.nkb_total, 8);
     a.k = k;
     a.kp = m->kp;
     a.N = N;
     a.ring = m->ring1;
-    a.coef = h->coef;
+    a.coef = coef;
     a.scales = m->scales;
     a.yt = m->yt;
-    a.yt_ld = h->n_snp_pad;
+    a.yt_ld = rows_pad;
     a.colmax = m->colmax;
     a.y_out = y_out;
     a.err = h->dflag;
     DPCA_CUDA(cudaMemsetAsync(m->colmax, 0, (size_t)k * 4, h->stream));
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
-        mixed_gemm_kernel<kXW><<<dim3(ceil_div(h->n_snp, 128), 1), kThreads, m->smem1, h->stream>>>(
-            m->map_p, m->map_om, a);
+        mixed_gemm_kernel<kXW><<<dim3(ceil_div(rows, 128), 1), kThreads, m->smem1, h->stream>>>(map_a, m->map_om, a);
         DPCA_CUDA(cudaGetLastError());
     }
     ScopedLaunch t(&h->clock, h->stream, "split_bop");
-    const int n16 = (h->n_snp + 15) & ~15;
-    int grid = std::min(ceil_div(n16, 256), h->sm_count * 8);
-    bop_split_kernel<<<grid, 256, 0, h->stream>>>(m->yt, h->n_snp_pad, h->n_snp, k, m->kp, N, h->coef, m->colmax,
-                                                   m->scales, m->bop);
+    const int n128 = (rows + 127) & ~127;
+    int grid = std::min(ceil_div(n128, 256), h->sm_count * 8);
+    bop_split_kernel<<<grid, 256, 0, h->stream>>>(m->yt, rows_pad, rows, k, m->kp, N, coef, m->colmax, m->scales,
+                                                   m->bop);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
 
-dpca_status launch_mixed_xty(Handle *h, double *z) {
+// Z (+)= X^T Y over `nsnp` SNPs (individual-major operand behind map_a, Y operand in m->bop).
+static dpca_status xty_rows(Handle *h, const CUtensorMap &map_a, int nsnp, double *z, bool accumulate) {
     MixedState *m = mstate(h);
-    const int k = h->k, N = m->N;
+    const int k = h->k;
+    int kb_per_split = m->kb_per_split, splits = m->splits;
+    if (nsnp != h->rows_dev) pick_splits(h, nsnp, &kb_per_split, &splits);
+    if (splits > m->splits_cap) {
+        kb_per_split = 8 * ceil_div(ceil_div(ceil_div(nsnp, 64), 8), m->splits_cap);
+        splits = ceil_div(ceil_div(nsnp, 64), kb_per_split);
+    }
     GemmArgs a{};
     a.rows = h->n_ind;
-    a.nkb_total = ceil_div(h->n_snp, 64);
-    a.kb_per_split = m->kb_per_split;
+    a.nkb_total = ceil_div(nsnp, 64);
+    a.kb_per_split = kb_per_split;
     a.k = k;
     a.kp = m->kp;
-    a.N = N;
+    a.N = m->N;
     a.ring = m->ring2;
     a.scales = m->scales;
     a.partial = m->partial;
     a.err = h->dflag;
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xty");
-        mixed_gemm_kernel<kXTY><<<dim3(ceil_div(h->n_ind, 128), m->splits), kThreads, m->smem2, h->stream>>>(
-            m->map_pt, m->map_bop, a);
+        mixed_gemm_kernel<kXTY><<<dim3(ceil_div(h->n_ind, 128), splits), kThreads, m->smem2, h->stream>>>(
+            map_a, m->map_bop, a);
         DPCA_CUDA(cudaGetLastError());
     }
     ScopedLaunch t(&h->clock, h->stream, "mixed_reduce");
     int64_t elems = (int64_t)h->n_ind * k;
     int grid = (int)std::min<int64_t>((elems + 255) / 256, (int64_t)h->sm_count * 8);
-    reduce_parts_kernel<<<grid, 256, 0, h->stream>>>(m->partial, elems, m->splits, z);
+    reduce_parts_kernel<<<grid, 256, 0, h->stream>>>(m->partial, elems, splits, z, accumulate ? 1 : 0);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
+}
+
+dpca_status launch_mixed_xw(Handle *h, const double *omega, double *y_out) {
+    DPCA_TRY(mixed_omega_operand(h, omega));
+    return xw_rows(h, mstate(h)->map_p[0], h->n_snp, h->coef, y_out);
+}
+
+dpca_status launch_mixed_xty(Handle *h, double *z) { return xty_rows(h, mstate(h)->map_pt[0], h->n_snp, z, false); }
+
+// One streamed block, rows [s0, s0 + ns) in buffer b: transpose it, Y_b = X_b Omega, then
+// z (+)= X_b^T Y_b.  The block's Y operand gets its own quantisation scales.
+dpca_status mixed_block(Handle *h, int b, int s0, int ns, double *z, bool accumulate) {
+    MixedState *m = mstate(h);
+    {
+        ScopedLaunch t(&h->clock, h->stream, "transpose_packed");
+        launch_transpose_raw(h->Pb[b], h->pitch, h->PTb[b], h->pitchTb, h->n_ind, ns, h->stream);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    DPCA_TRY(xw_rows(h, m->map_p[b], ns, h->coef + 2 * (size_t)s0, nullptr));
+    return xty_rows(h, m->map_pt[b], ns, z, accumulate);
 }
 
 }  // namespace dpca

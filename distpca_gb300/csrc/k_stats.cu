@@ -87,13 +87,14 @@ dpca_status launch_snp_stats(Handle *h) {
     return DPCA_OK;
 }
 
-// The statistics kernel on caller-given buffers: used by the allocation-free pass, whose
-// buffers live in a static device array rather than in a handle.
-void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, int32_t *counts, double *avg,
-                          double *sd, double *lut, cudaStream_t stream) {
+// The statistics kernel on caller-given buffers: used by the allocation-free pass and by the
+// streaming sweep, whose rows are one block of the matrix (inv_sqrt_nsnp is then the whole
+// matrix's 1/sqrt(n_snp)).
+void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, double inv_sqrt_nsnp,
+                          int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream) {
     const int64_t np = ((int64_t)n_ind + 3) / 4;
-    snp_stats_kernel<<<ceil_div(n_snp, 8), 256, 0, stream>>>(P, pitch, n_ind, n_snp, np, 1.0 / sqrt((double)n_snp),
-                                                            counts, avg, sd, lut, nullptr);
+    snp_stats_kernel<<<ceil_div(n_snp, 8), 256, 0, stream>>>(P, pitch, n_ind, n_snp, np, inv_sqrt_nsnp, counts, avg,
+                                                            sd, lut, coef);
 }
 
 // One thread writes one 32-bit word (16 individuals) of one SNP row; the
@@ -184,6 +185,12 @@ __global__ void __launch_bounds__(256) transpose_packed_kernel(const uint8_t *__
         int64_t byte0 = (int64_t)(s0 >> 2);
         *reinterpret_cast<uint4 *>(PT + (int64_t)i * pitchT + byte0) = make_uint4(out[0], out[1], out[2], out[3]);
     }
+}
+
+void launch_transpose_raw(const uint8_t *P, int64_t pitch, uint8_t *PT, int64_t pitchT, int n_ind, int n_snp,
+                          cudaStream_t stream) {
+    dim3 grid(ceil_div(n_ind, kTI), ceil_div(n_snp, kTS));
+    transpose_packed_kernel<<<grid, 256, 0, stream>>>(P, pitch, PT, pitchT, n_ind, n_snp);
 }
 
 dpca_status launch_transpose_packed(Handle *h) {

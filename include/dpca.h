@@ -76,9 +76,9 @@ typedef struct {
     char prefix[1024]; /* -prefix  output prefix (default "noprefix") */
     int precision;     /* dpca_precision (default DPCA_PREC_MIXED) */
     int device;        /* CUDA device ordinal (default 0) */
-    double hbm_budget_gb; /* reserved for block streaming from pinned host memory, which this version does
-                             not implement: a packed matrix that does not fit the device fails with
-                             DPCA_ERR_NOMEM */
+    double hbm_budget_gb; /* -hbm: device bytes (GB) the resident packed matrix may use; above it (or,
+                             when 0, above 85% of the free device memory) dpca_run streams the rows
+                             from host memory in blocks */
 } dpca_config;
 
 /* Results and the reference's timers (seconds).  sigma and u are caller-owned. */
@@ -88,7 +88,7 @@ typedef struct {
     int total_its;      /* outer iterations performed */
     int passes;         /* applications of X^T X */
     int in_core;        /* 1 when the in-core variant's Gram-form Rayleigh quotient was used */
-    int streamed;       /* 1 when packed blocks were streamed from host memory each pass (always 0 here) */
+    int streamed;       /* 1 when packed blocks were streamed from host memory each pass */
     double *sigma;      /* [nsv]            singular values (sqrt of Ritz values) */
     double *u;          /* [n_ind * nsv]    left singular vectors, row-major */
     double *delta_iter; /* [miter] or NULL  sum of sigma per iteration */
@@ -125,6 +125,14 @@ void dpca_print_statistics(const dpca_config *cfg, const dpca_result *res);
 /* ---- device-resident handle ---- */
 /* stream: a cudaStream_t to order work on, or NULL for a handle-owned stream. */
 dpca_status dpca_create(dpca_handle **h, int n_ind, int n_snp, int nrhs, int precision, int device, void *stream);
+/* Streaming handle (the out-of-core block reader, src/methods.cpp:795-811, 873-874): the device
+ * holds two blocks of block_snps SNP rows (rounded up to 128) and, on the mixed path, their
+ * transposes.  dpca_upload then only records the host rows, which must stay valid and unchanged
+ * until the handle is destroyed (pinned memory copies at full speed), and computes the per-SNP
+ * statistics in one sweep; every pass copies the blocks in on a side stream, double-buffered,
+ * and accumulates Z over them.  dpca_synth_fill is not available on such a handle. */
+dpca_status dpca_create_streamed(dpca_handle **h, int n_ind, int n_snp, int nrhs, int precision, int device,
+                                 void *stream, int block_snps);
 dpca_status dpca_destroy(dpca_handle *h);
 /* Copy packed rows (host, pinned or pageable) to the device and compute per-SNP statistics. */
 dpca_status dpca_upload(dpca_handle *h, const uint8_t *packed, int64_t row_stride);
