@@ -17,7 +17,7 @@ import numpy as np
 
 __all__ = ["DpcaError", "Config", "Result", "Handle", "lib", "library_path", "config", "parse_args", "probe",
            "resolve", "start_block", "run", "run_packed", "decode_counts", "PREC_FP64", "PREC_MIXED",
-           "exported_symbols"]
+           "exported_symbols", "FullSVD", "full_svd"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PREC_FP64 = 0
@@ -52,7 +52,9 @@ class Result(ctypes.Structure):
                 ("delta_iter", _D), ("time_generate_rhs", ctypes.c_double), ("time_load_matrix", ctypes.c_double),
                 ("time_mm", ctypes.c_double), ("time_mm_a", ctypes.c_double), ("time_mm_a_t", ctypes.c_double),
                 ("time_gs", ctypes.c_double), ("time_projected_svd", ctypes.c_double),
-                ("time_other", ctypes.c_double), ("time_total", ctypes.c_double)]
+                ("time_other", ctypes.c_double), ("time_total", ctypes.c_double),
+                ("time_true_svd", ctypes.c_double), ("frob_norm_angle", ctypes.c_double),
+                ("cos_error", ctypes.c_double)]
 
 
 def library_path() -> str:
@@ -98,6 +100,10 @@ _SIGS = {
     "dpca_reset_kernel_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dpca_pass_fp64_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                                ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "dpca_full_svd": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "dpca_write_fullsvd": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p]),
     "dpca_decode_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
 }
@@ -341,3 +347,42 @@ class Handle:
 
     def reset_kernel_times(self, enable: bool = True) -> None:
         _check(lib().dpca_reset_kernel_times(self._h, 1 if enable else 0))
+
+
+class FullSVD(ctypes.Structure):
+    _fields_ = [("info", ctypes.c_int), ("time_true_svd", ctypes.c_double), ("frob_norm_angle", ctypes.c_double),
+                ("cos_error", ctypes.c_double), ("true_sigma", _D), ("true_u", _D), ("sigma_relerr", _D),
+                ("vec_relerr", _D), ("cosines", _D)]
+
+
+def full_svd(result: Dict, n_ind: int, n_snp: int, packed: Optional[np.ndarray] = None, bfile: Optional[str] = None,
+             write: bool = False, **flags) -> Dict:
+    """-fullSVD check of a result (sigma, u) against the dense SVD of the standardized matrix."""
+    c = config(**flags)
+    nsv = len(result["sigma"])
+    sigma = np.ascontiguousarray(result["sigma"], dtype=np.float64)
+    u = np.ascontiguousarray(result["u"], dtype=np.float64)
+    r = Result()
+    r.n_ind, r.n_snp, r.nsv, r.nrhs = n_ind, n_snp, nsv, c.nrhs
+    r.sigma = sigma.ctypes.data_as(_D)
+    r.u = u.ctypes.data_as(_D)
+    out = {k: np.zeros(n) for k, n in (("true_sigma", nsv), ("true_u", n_ind * nsv), ("sigma_relerr", nsv),
+                                         ("vec_relerr", n_ind * nsv), ("cosines", nsv))}
+    f = FullSVD()
+    for k, a in out.items():
+        setattr(f, k, a.ctypes.data_as(_D))
+    if packed is not None:
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        st = lib().dpca_full_svd(ctypes.byref(c), None, _p(packed), packed.shape[1], n_ind, n_snp, ctypes.byref(r),
+                                 ctypes.byref(f))
+    else:
+        st = lib().dpca_full_svd(ctypes.byref(c), bfile.encode(), None, 0, n_ind, n_snp, ctypes.byref(r),
+                                 ctypes.byref(f))
+    _check(st)
+    if write:
+        _check(lib().dpca_write_fullsvd(ctypes.byref(c), bfile.encode() if bfile else None, n_ind, nsv,
+                                        ctypes.byref(f)))
+    out["true_u"] = out["true_u"].reshape(n_ind, nsv)
+    out["vec_relerr"] = out["vec_relerr"].reshape(n_ind, nsv)
+    out.update(info=f.info, time_true_svd=f.time_true_svd, frob_norm_angle=f.frob_norm_angle, cos_error=f.cos_error)
+    return out

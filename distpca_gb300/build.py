@@ -22,7 +22,7 @@ LIB = os.path.join(OUT, "libdpca.so")
 CLI = os.path.join(OUT, "dpca")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["k_stats.cu", "k_fp64.cu", "k_dense.cu", "k_mixed.cu", "handle.cu"]
+CU_SOURCES = ["k_stats.cu", "k_fp64.cu", "k_dense.cu", "k_mixed.cu", "k_fullsvd.cu", "handle.cu"]
 CPP_SOURCES = ["host.cpp"]
 
 
@@ -80,8 +80,10 @@ def build(verbose: bool = False, jobs: int = 0) -> str:
                 f.result()
     if _stale(LIB, objs):
         tmp = LIB + f".tmp{os.getpid()}"
-        subprocess.check_call([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-ldl",
-                               "-lpthread"])
+        # cuSOLVER (dense eigensolve of the -fullSVD check) is a shared library of the toolkit
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
+        subprocess.check_call([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lcusolver",
+                               "-Xlinker", f"-rpath={cuda_lib}", "-lrt", "-ldl", "-lpthread"])
         os.replace(tmp, LIB)
     cli_src = os.path.join(CSRC, "cli.cpp")
     if _stale(CLI, [cli_src, LIB] + heads):

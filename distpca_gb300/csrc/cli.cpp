@@ -110,5 +110,22 @@ int main(int argc, char **argv) {
         }
     }
     if (cfg.verbose > 0) dpca_print_statistics(&cfg, &res);
+    if (cfg.full_svd == 1) {
+        // distpca.cpp:449-635: after the statistics block, the dense check and its files
+        std::vector<double> ts(res.nsv), tu((size_t)M * res.nsv), se(res.nsv), ve((size_t)M * res.nsv), cs(res.nsv);
+        dpca_fullsvd fs;
+        memset(&fs, 0, sizeof(fs));
+        fs.true_sigma = ts.data();
+        fs.true_u = tu.data();
+        fs.sigma_relerr = se.data();
+        fs.vec_relerr = ve.data();
+        fs.cosines = cs.data();
+        st = dpca_full_svd(&cfg, bfile, nullptr, 0, M, N, &res, &fs);
+        if (st != DPCA_OK) return fail(st);
+        if (cfg.fwrite == 1) {
+            st = dpca_write_fullsvd(&cfg, bfile, M, res.nsv, &fs);
+            if (st != DPCA_OK) return fail(st);
+        }
+    }
     return 0;
 }

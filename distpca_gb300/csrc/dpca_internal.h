@@ -109,6 +109,8 @@ struct Handle {
     uint8_t *Pb[2] = {nullptr, nullptr};   // block buffers, blk x pitch
     uint8_t *PTb[2] = {nullptr, nullptr};  // mixed: block transposes, n_ind x pitchTb
     int64_t pitchTb = 0;
+    uint8_t *Sb[2] = {nullptr, nullptr};   // staging for one contiguous host copy per block (host rows
+                                           // whose stride is not the device pitch), re-pitched on device
     cudaStream_t cstream = nullptr;        // copy stream
     cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
 
@@ -141,6 +143,9 @@ void launch_transpose_raw(const uint8_t *P, int64_t pitch, uint8_t *PT, int64_t 
 // one streamed block: Z (+)= X_b^T (X_b Omega) over SNP rows [s0, s0 + ns) held in buffer b
 dpca_status launch_fp64_block(Handle *h, int b, int s0, int ns, const double *omega, double *z, bool accumulate);
 dpca_status mixed_omega_operand(Handle *h, const double *omega);
+// -fullSVD: leading nsv singular values / left vectors (host, n_ind x nsv) of a resident FP64
+// handle created with nrhs = 128
+dpca_status full_svd_device(Handle *h, int nsv, double *sigma, double *u, int *info);
 dpca_status mixed_block(Handle *h, int b, int s0, int ns, double *z, bool accumulate);
 dpca_status launch_fp64_xw(Handle *h, const double *omega, double *y);
 dpca_status launch_fp64_xty(Handle *h, const double *y, double *z);

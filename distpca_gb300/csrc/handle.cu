@@ -100,7 +100,8 @@ static void free_all(Handle *h) {
     if (h->mx) mixed_release(h);
     void *ptrs[] = {h->P,     h->PT,    h->counts, h->avg,      h->sd,  h->lut,    h->coef,
                     h->omega, h->z,     h->q,      h->old,      h->work, h->y,     h->partial,
-                    h->small, h->red,   h->dflag,  h->Pb[0],    h->Pb[1], h->PTb[0], h->PTb[1]};
+                    h->small, h->red,   h->dflag,  h->Pb[0],    h->Pb[1], h->PTb[0], h->PTb[1],
+                    h->Sb[0], h->Sb[1]};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int b = 0; b < 2; ++b) {
@@ -228,8 +229,17 @@ static dpca_status stream_in(Handle *h, int j, int *s0, int *ns) {
     *s0 = j * h->blk;
     *ns = std::min(h->blk, h->n_snp - *s0);
     DPCA_CUDA(cudaStreamWaitEvent(h->cstream, h->consumed[b], 0));
-    DPCA_CUDA(cudaMemcpy2DAsync(h->Pb[b], h->pitch, h->hostP + (int64_t)*s0 * h->host_stride, h->host_stride, h->np,
-                                *ns, cudaMemcpyHostToDevice, h->cstream));
+    const uint8_t *src = h->hostP + (int64_t)*s0 * h->host_stride;
+    if (h->Sb[b]) {
+        // host rows are not at the device pitch: one contiguous copy (full link speed; a
+        // row-pitched host copy ran ~35% slower), then a device-side re-pitch
+        DPCA_CUDA(cudaMemcpyAsync(h->Sb[b], src, (size_t)*ns * h->host_stride, cudaMemcpyHostToDevice, h->cstream));
+        DPCA_CUDA(cudaMemcpy2DAsync(h->Pb[b], h->pitch, h->Sb[b], h->host_stride, h->np, *ns,
+                                    cudaMemcpyDeviceToDevice, h->cstream));
+    } else {
+        DPCA_CUDA(cudaMemcpy2DAsync(h->Pb[b], h->pitch, src, h->host_stride, h->np, *ns, cudaMemcpyHostToDevice,
+                                    h->cstream));
+    }
     DPCA_CUDA(cudaEventRecord(h->copied[b], h->cstream));
     DPCA_CUDA(cudaStreamWaitEvent(h->stream, h->copied[b], 0));
     return DPCA_OK;
@@ -503,6 +513,13 @@ dpca_status dpca_upload(dpca_handle *hh, const uint8_t *packed, int64_t row_stri
         // the rows stay in host memory and are read block by block in every pass
         h->hostP = packed;
         h->host_stride = row_stride;
+        if (row_stride != h->pitch) {
+            for (int b = 0; b < 2; ++b) {
+                if (h->Sb[b]) cudaFree(h->Sb[b]);
+                h->Sb[b] = nullptr;
+                DPCA_TRY(dalloc(&h->Sb[b], (size_t)h->blk * row_stride));
+            }
+        }
         DPCA_TRY(after_data(h));
         return DPCA_OK;
     }

@@ -116,6 +116,47 @@ static std::string pure_name(const std::string &full) {
     return dot == std::string::npos ? base : base.substr(0, dot);
 }
 
+// Largest singular value of a small square matrix C (k x k, row-major): sqrt of the largest
+// eigenvalue of C^T C by cyclic Jacobi.  Used by the -fullSVD report (computeCosineError takes
+// the first singular value of (Uhat^T U with |diagonal| - I), utilities.cpp:262-265).
+static double largest_singular_value(const std::vector<double> &C, int k) {
+    std::vector<double> A((size_t)k * k, 0.0);
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) {
+            double s = 0;
+            for (int r = 0; r < k; ++r) s += C[(size_t)r * k + i] * C[(size_t)r * k + j];
+            A[(size_t)i * k + j] = s;
+        }
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0;
+        for (int p = 0; p < k; ++p)
+            for (int q = p + 1; q < k; ++q) off += A[(size_t)p * k + q] * A[(size_t)p * k + q];
+        if (off < 1e-30) break;
+        for (int p = 0; p < k; ++p)
+            for (int q = p + 1; q < k; ++q) {
+                const double apq = A[(size_t)p * k + q];
+                if (apq == 0.0) continue;
+                const double app = A[(size_t)p * k + p], aqq = A[(size_t)q * k + q];
+                const double theta = (aqq - app) / (2 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+                const double c = 1 / std::sqrt(t * t + 1), sn = t * c;
+                for (int r = 0; r < k; ++r) {
+                    const double arp = A[(size_t)r * k + p], arq = A[(size_t)r * k + q];
+                    A[(size_t)r * k + p] = c * arp - sn * arq;
+                    A[(size_t)r * k + q] = sn * arp + c * arq;
+                }
+                for (int r = 0; r < k; ++r) {
+                    const double apr = A[(size_t)p * k + r], aqr = A[(size_t)q * k + r];
+                    A[(size_t)p * k + r] = c * apr - sn * aqr;
+                    A[(size_t)q * k + r] = sn * apr + c * aqr;
+                }
+            }
+    }
+    double mx = 0;
+    for (int i = 0; i < k; ++i) mx = std::max(mx, A[(size_t)i * k + i]);
+    return std::sqrt(std::max(mx, 0.0));
+}
+
 static dpca_status run_common(const dpca_config *cfg_in, const char *bfile, const uint8_t *packed_host,
                               int64_t row_stride, int n_ind, int n_snp, double *omega_inout, dpca_result *res) {
     if (!cfg_in || !omega_inout || !res) {
@@ -459,6 +500,118 @@ dpca_status dpca_write_outputs(const dpca_config *cfg, const char *bfile, const 
     return DPCA_OK;
 }
 
+dpca_status dpca_full_svd(const dpca_config *cfg, const char *bfile, const uint8_t *packed, int64_t row_stride,
+                          int n_ind, int n_snp, const dpca_result *res, dpca_fullsvd *out) {
+    clear_error();
+    if (!cfg || !res || !out || !res->sigma || !res->u || !out->true_sigma || !out->sigma_relerr || !out->cosines ||
+        n_ind <= 0 || n_snp <= 0 || (!packed && !bfile)) {
+        set_error("dpca_full_svd: null argument or empty matrix");
+        return DPCA_ERR_INVALID;
+    }
+    const int nsv = res->nsv;
+    if (n_ind > 20000) {
+        set_error("-fullSVD: the dense check supports up to 20000 individuals (got %d)", n_ind);
+        return DPCA_ERR_UNSUPPORTED;
+    }
+    if (nsv < 1 || nsv > std::min(n_ind, n_snp)) {
+        set_error("-fullSVD: nsv %d outside [1, min(n_ind, n_snp)]", nsv);
+        return DPCA_ERR_INVALID;
+    }
+    const int64_t np = (n_ind + 3) / 4;
+    std::vector<uint8_t> filebuf;
+    const uint8_t *src = packed;
+    int64_t stride = row_stride;
+    if (!src) {
+        std::string bed = std::string(bfile) + ".bed";
+        int fd = open(bed.c_str(), O_RDONLY);
+        if (fd < 0) {
+            set_error("[Data::read_bed] Error reading file %s", bed.c_str());
+            return DPCA_ERR_IO;
+        }
+        filebuf.resize((size_t)np * n_snp);
+        dpca_status st = pread_all(fd, filebuf.data(), filebuf.size(), 3, bed.c_str());
+        close(fd);
+        DPCA_TRY(st);
+        src = filebuf.data();
+        stride = np;
+    }
+    dpca_handle *hh = nullptr;
+    DPCA_TRY(dpca_create(&hh, n_ind, n_snp, 128, DPCA_PREC_FP64, cfg->device, nullptr));
+    dpca_status st = dpca_upload(hh, src, stride);
+    std::vector<double> tu((size_t)n_ind * nsv);
+    const double t0 = wall_now();
+    if (st == DPCA_OK) st = full_svd_device(&hh->h, nsv, out->true_sigma, tu.data(), &out->info);
+    out->time_true_svd = wall_now() - t0;
+    dpca_destroy(hh);
+    DPCA_TRY(st);
+    // comparisons as distpca.cpp:522-557 and computeCosineError (utilities.cpp:234-270)
+    for (int i = 0; i < nsv; ++i) {
+        const double denom = out->true_sigma[i] ? out->true_sigma[i] : 1.0;
+        out->sigma_relerr[i] = std::fabs(out->true_sigma[i] - res->sigma[i]) / denom;
+    }
+    if (out->true_u) memcpy(out->true_u, tu.data(), tu.size() * sizeof(double));
+    if (out->vec_relerr)
+        for (size_t e = 0; e < tu.size(); ++e)
+            out->vec_relerr[e] = std::fabs(std::fabs(tu[e]) - std::fabs(res->u[e])) / (std::fabs(tu[e]) + 1e-12);
+    std::vector<double> C((size_t)nsv * nsv, 0.0);  // Uhat^T U
+    for (int i = 0; i < n_ind; ++i)
+        for (int a = 0; a < nsv; ++a) {
+            const double ua = res->u[(size_t)i * nsv + a];
+            for (int b = 0; b < nsv; ++b) C[(size_t)a * nsv + b] += ua * tu[(size_t)i * nsv + b];
+        }
+    double frob = 0;
+    for (int a = 0; a < nsv; ++a)
+        for (int b = 0; b < nsv; ++b) {
+            const double v = C[(size_t)a * nsv + b];
+            frob += a == b ? (std::fabs(v) - 1.0) * (std::fabs(v) - 1.0) : v * v;
+        }
+    out->frob_norm_angle = std::sqrt(frob);
+    for (int a = 0; a < nsv; ++a) {
+        out->cosines[a] = C[(size_t)a * nsv + a];
+        C[(size_t)a * nsv + a] = std::fabs(C[(size_t)a * nsv + a]) - 1.0;
+    }
+    out->cos_error = largest_singular_value(C, nsv);
+    if (cfg->verbose > 1) {
+        printf("\nFULL SVD computed in %lf sec, info = %d\n\n", out->time_true_svd, out->info);
+        for (int i = 0; i < nsv; ++i) printf("RelError Sigma(%d): %e\n", i, out->sigma_relerr[i]);
+        for (int i = 0; i < nsv; ++i) printf("Cosine(%d): %lf\n", i, out->cosines[i]);
+    }
+    return DPCA_OK;
+}
+
+dpca_status dpca_write_fullsvd(const dpca_config *cfg, const char *bfile, int n_ind, int nsv,
+                               const dpca_fullsvd *fs) {
+    clear_error();
+    if (!cfg || !fs || !fs->true_sigma || !fs->true_u || !fs->vec_relerr || !fs->cosines) {
+        set_error("dpca_write_fullsvd: the check's vectors are needed (true_u, vec_relerr)");
+        return DPCA_ERR_INVALID;
+    }
+    std::string prefix(cfg->prefix);
+    std::string pure = pure_name(bfile ? bfile : "noprefix");
+    auto name = [&](const char *type) {
+        return prefix.empty() ? construct_filename(pure, type) : prefix + "_" + type + ".txt";
+    };
+    FILE *fvec = fopen(name("realLeftSingularVectors").c_str(), "w");
+    FILE *fval = fopen(name("realSingularValues").c_str(), "w");
+    FILE *ferr = fopen(name("singvecs_accuracy").c_str(), "w");
+    FILE *fcos = fopen(name("cosineValues").c_str(), "w");
+    if (!fvec || !fval || !ferr || !fcos) {
+        for (FILE *f : {fvec, fval, ferr, fcos})
+            if (f) fclose(f);
+        set_error("File error");
+        return DPCA_ERR_IO;
+    }
+    for (int i = 0; i < n_ind; ++i) {
+        for (int j = 0; j < nsv; ++j) fprintf(fvec, "%2.13f ", fs->true_u[(size_t)i * nsv + j]);
+        fprintf(fvec, "\n");
+    }
+    for (int i = 0; i < nsv; ++i) fprintf(fval, "%2.13f\n", fs->true_sigma[i]);
+    for (size_t i = 0; i < (size_t)n_ind * nsv; ++i) fprintf(ferr, "%2.13lf\n", fs->vec_relerr[i]);
+    for (int i = 0; i < nsv; ++i) fprintf(fcos, "%2.13lf\n", fs->cosines[i]);
+    for (FILE *f : {fvec, fval, ferr, fcos}) fclose(f);
+    return DPCA_OK;
+}
+
 // print_statistics (utilities.cpp:147-193), same lines and formats.
 void dpca_print_statistics(const dpca_config *cfg, const dpca_result *r) {
     time_t raw;
@@ -507,6 +660,13 @@ void dpca_print_statistics(const dpca_config *cfg, const dpca_result *r) {
             printf("Total wall-clock time elapsed (without including the time spent on loading the matrix): "
                    "%02.13f\n",
                    noload / d);
+    }
+    // utilities.cpp:187-191: printed for in-core runs with -fullSVD; the reference prints these
+    // before the check runs, so they read zero unless a caller filled them in first
+    if (cfg && cfg->full_svd == 1 && r->rows_fetched == r->n_snp) {
+        printf("\nTotal wall-clock time to compute the full ('econ') SVD: %02.13f\n", r->time_true_svd);
+        printf("||Uhat^TU - I||_F: %02.13f\n", r->frob_norm_angle);
+        printf("||Uhat^TU - I||_2: %02.13f\n", r->cos_error);
     }
 }
 

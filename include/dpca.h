@@ -94,7 +94,24 @@ typedef struct {
     double *delta_iter; /* [miter] or NULL  sum of sigma per iteration */
     double time_generate_rhs, time_load_matrix, time_mm, time_mm_a, time_mm_a_t;
     double time_gs, time_projected_svd, time_other, time_total;
+    /* -fullSVD results as the statistics block reports them (distpca.cpp's TIME_2_TRUE_SVD,
+     * frob_norm_angle, cos_error); zero until dpca_full_svd fills a dpca_fullsvd */
+    double time_true_svd, frob_norm_angle, cos_error;
 } dpca_result;
+
+/* The -fullSVD accuracy check: the dense SVD of the standardized matrix compared with a result.
+ * Arrays are caller-owned; true_u and vec_relerr may be NULL. */
+typedef struct {
+    int info;              /* 0 on success (the eigensolver's info otherwise) */
+    double time_true_svd;  /* seconds for the dense decomposition */
+    double frob_norm_angle;/* ||(Uhat^T U) with |diagonal| - I||_F */
+    double cos_error;      /* ||(Uhat^T U) with |diagonal| - I||_2 */
+    double *true_sigma;    /* [nsv] leading singular values */
+    double *true_u;        /* [n_ind * nsv] leading left singular vectors, row-major */
+    double *sigma_relerr;  /* [nsv] |sigma_true - sigma| / sigma_true */
+    double *vec_relerr;    /* [n_ind * nsv] ||u_true| - |u|| / (|u_true| + 1e-12) */
+    double *cosines;       /* [nsv] diagonal of Uhat^T U */
+} dpca_fullsvd;
 
 typedef struct dpca_handle dpca_handle;
 
@@ -121,6 +138,17 @@ dpca_status dpca_run_packed(const dpca_config *cfg, const uint8_t *packed, int64
 /* Write <prefix>_singularValues.txt and <prefix>_leftSingularVectors.txt (IIDs from <bfile>.fam). */
 dpca_status dpca_write_outputs(const dpca_config *cfg, const char *bfile, const dpca_result *res);
 void dpca_print_statistics(const dpca_config *cfg, const dpca_result *res);
+/* -fullSVD (distpca.cpp:449-635, computeCosineError utilities.cpp:234-270): the dense SVD of the
+ * standardized matrix on the device -- the FP64 Gram matrix X^T X (n_ind x n_ind) from the packed
+ * rows and its symmetric eigendecomposition -- compared with res (sigma, u).  Rows come from
+ * packed (host, row_stride apart) or, when packed is NULL, from <bfile>.bed.  n_ind is limited
+ * to 20,000 (DPCA_ERR_UNSUPPORTED above).  With verbose > 1 it prints the reference's lines. */
+dpca_status dpca_full_svd(const dpca_config *cfg, const char *bfile, const uint8_t *packed, int64_t row_stride,
+                          int n_ind, int n_snp, const dpca_result *res, dpca_fullsvd *out);
+/* The four -fullSVD -fwrite files: <prefix>_realLeftSingularVectors.txt, _realSingularValues.txt,
+ * _singvecs_accuracy.txt, _cosineValues.txt (timestamped names without a prefix). */
+dpca_status dpca_write_fullsvd(const dpca_config *cfg, const char *bfile, int n_ind, int nsv,
+                               const dpca_fullsvd *f);
 
 /* ---- device-resident handle ---- */
 /* stream: a cudaStream_t to order work on, or NULL for a handle-owned stream. */

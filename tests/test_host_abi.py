@@ -170,3 +170,12 @@ def test_no_device_is_a_loud_error(dpca):
     prefix, n_ind, n_snp, packed = fileset("tiny")
     with pytest.raises(dpca.DpcaError):
         dpca.decode_counts(packed, n_ind)
+
+
+def test_full_svd_limits_checked_before_the_device(dpca):
+    # the dense check refuses large cohorts up front (no GPU needed to reach the error)
+    r = {"sigma": np.ones(3), "u": np.zeros((30_000, 3))}
+    packed = np.zeros((4, 7500), dtype=np.uint8)
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.full_svd(r, 30_000, 4, packed=packed, nsv=3, nrhs=6)
+    assert e.value.status == 6
