@@ -1,29 +1,33 @@
 // Mixed-precision pass on the 5th-generation tensor cores (tcgen05), sm_103a.
 //
 // The standardized matrix is never materialised.  With g' = genotype (0/1/2, 0 when missing),
-// m = 1 for non-missing entries, and per-SNP b = 1/(sd*sqrt(n_snp)), a = -avg*b,
-//     X[s,i] = b_s g'[s,i] + a_s m[s,i]          (the value standardize() gives, utilities.cpp:294-305)
-// so the two products of the pass (methods.cpp:853-854, 862-863) become
-//     Y  = X Omega  = diag(b) (G' Omega) + diag(a) (M Omega)                      (gemm<kXW>)
-//     Z  = X^T Y    = G'^T (b.Y) + M^T (a.Y)                                      (gemm<kXTY>)
+// miss = 1 for missing entries, and per-SNP b = 1/(sd*sqrt(n_snp)), a = -avg*b, the value
+// standardize() gives (utilities.cpp:294-305) is X = b g' + a (1 - miss).  Written with
+//     f1 = g' - miss  in {0, -1, 1, 2} for codes 00, 01, 10, 11,   f2 = relu(f1) = g',
+// it is X[s,i] = a_s + a_s f1[s,i] + (b_s - a_s) f2[s,i]: one table lookup per pair of codes
+// (f1) and one FP16 max (f2) per pair.  The two products of the pass (methods.cpp:853-854,
+// 862-863) become
+//     Y  = X Omega  = diag(a) (F1 Omega + 1 colsum(Omega)^T) + diag(b - a) (F2 Omega)   (gemm<kXW>)
+//     Z  = X^T Y    = F1^T (a.Y) + F2^T ((b - a).Y) + 1 (sum_s a_s Y_s)^T               (gemm<kXTY>)
+// where the rank-one terms are exact integer sums of the same quantised operands.
 //
 // Exactness.  The tensor core adds into its FP32 accumulator with truncation (round toward
 // zero), which biases long sums.  So every product and partial sum is made an integer below 2^24,
 // where truncation cannot lose a bit:
-//   - G' and M are exact small integers in FP16;
-//   - each dense operand column (Omega; b.Y and a.Y) is scaled by the power of two that puts its
-//     largest magnitude just under 2^23 and rounded to the nearest integer v (24-bit fixed
+//   - f1 and f2 are exact small integers in FP16;
+//   - each dense operand column (Omega; a.Y and (b-a).Y) is scaled by the power of two that puts
+//     its largest magnitude just under 2^23 and rounded to the nearest integer v (24-bit fixed
 //     point, an unbiased quantisation), stored as two integer FP16 slices v = 4096 h + l with
 //     h, l in [-2048, 2048] (FP16 holds every such integer exactly), laid side by side along the
 //     MMA's N dimension ([h | l], N = 2*round_up(k, 8));
-//   - the G' and M products have one TMEM accumulator each; an accumulator sums a bounded
+//   - the f2 and f1 products have one TMEM accumulator each; an accumulator sums a bounded
 //     number of K-blocks (a chunk) so that every partial sum stays within 2^24, then the drain
 //     warps copy it to registers, release it, and fold the exact integer 4096 h + l into 64-bit
-//     integer accumulators in shared memory.  The M chunks end half a G' chunk later than the
-//     G' chunks, so the tensor core keeps working on one product while the other is drained.
+//     integer accumulators in shared memory.  The f1 chunks end half a chunk later than the f2
+//     chunks, so the tensor core keeps working on one product while the other is drained.
 // The per-SNP coefficients and the scale removal are applied once per output, in FP64.  The
-// X Omega epilogue writes Y (FP32, transposed) and the exact column maxima of |b.Y|, |a.Y|, from
-// which a split kernel quantises the X^T Y operand.
+// X Omega epilogue writes Y (FP32, transposed) and the exact column maxima of |a.Y|, |(b-a).Y|,
+// from which a split kernel quantises the X^T Y operand.
 //
 // Pipeline step = one batch of two 64-element K-blocks (8 MMA K-steps per product).  Batching
 // matters: an MMA-issuing thread spends ~150 cycles on each barrier wait and ~45 on each
@@ -36,7 +40,7 @@
 //                swizzled.
 //   warps 1, 14  TMEM allocation (warp 1) and the two MMA-issuing threads
 //                (tcgen05.mma.kind::f16, A from tensor memory, B from shared memory): warp 1
-//                issues the G' products, warp 14 the M products, each into its own accumulator.
+//                issues the f2 products, warp 14 the f1 products, each into its own accumulator.
 //   warps 2..9   decode, two groups of four warps, each owning one TMEM A stage and taking
 //                alternate batches: one thread per tile row turns 2 x 16 packed bytes into
 //                FP16 pairs with byte-permute table lookups and stores them (tcgen05.st).
@@ -66,13 +70,13 @@ constexpr int kPStageBytes = 128 * 128;  // 128 rows x 128 B = 512 K-elements = 
 constexpr int kTmemCols = 512;
 constexpr int kSmemFloor = 120 * 1024;   // keeps one CTA per SM (the CTA owns all of TMEM)
 constexpr int kSmemBudget = 220 * 1024;
-// Batches per exact accumulation chunk.  A batch is 8 K steps of 16 products; a G' product
-// term is at most 2 * 2048 in magnitude, so a batch adds at most 2^19 and 32 batches at most
-// 2^24; an M term is at most 2048, allowing 64 batches.  Every partial sum is then an integer
-// of magnitude <= 2^24, which the FP32 accumulator holds exactly whatever the summation order.
-constexpr int kChunkG = 32;
-constexpr int kChunkM = 64;
-constexpr int kFirstChunkM = 48;         // staggers the M drains against the G' drains
+// Batches per exact accumulation chunk.  A batch is 8 K steps of 16 products; an f1 or f2
+// product term is at most 2 * 2048 in magnitude, so a batch adds at most 2^19 and 32 batches at
+// most 2^24.  Every partial sum is then an integer of magnitude <= 2^24, which the FP32
+// accumulator holds exactly whatever the summation order.
+constexpr int kChunkG = 32;              // f2 (= g') accumulator
+constexpr int kChunkM = 32;              // f1 accumulator
+constexpr int kFirstChunkM = 48;         // staggers the f1 drains against the f2 drains
 constexpr int kMaxMixedNrhs = 48;        // accumulators 2 x N <= 192 columns + 2 A stages of 128
 
 struct GemmArgs {
@@ -85,7 +89,8 @@ struct GemmArgs {
     const double *scales;   // [4][k]: omega scale, its inverse, b/aY scale, its inverse
     float *yt;              // kXW: Y transposed, [k][yt_ld] (FP32)
     int64_t yt_ld;
-    unsigned int *colmax;   // kXW: per column, bits of max(|b.Y|, |a.Y|) (non-negative float)
+    unsigned int *colmax;   // kXW: per column, bits of max(|a.Y|, |(b-a).Y|) (non-negative float)
+    const long long *colsumq;  // kXW: per column, sum over individuals of the quantised Omega
     double *y_out;          // kXW: optional FP64 Y [rows][k]
     double *partial;        // kXTY: [splits][rows][k]
     int *err;
@@ -97,6 +102,8 @@ struct MixedState {
     __half *bop = nullptr;      // [2N][n_snp_pad]
     float *yt = nullptr;        // [k][n_snp_pad]
     unsigned int *colmax = nullptr;  // [k]
+    long long *colsumq = nullptr;    // [k] sum of the quantised Omega column (integers)
+    long long *rq = nullptr;         // [k] sum over SNPs of the quantised a.Y column (integers)
     double *scales = nullptr;   // [4][k]
     double *partial = nullptr;  // [splits][n_ind][k]
     int splits = 1, kb_per_split = 8;
@@ -114,13 +121,18 @@ struct MixedState {
 // perm16(L) of that group.
 __host__ __device__ __forceinline__ int perm16(int L) { return ((L >> 1) & 3) + 8 * (L >> 3) + 4 * (L & 1); }
 
-// 16 packed bytes = 64 codes -> FP16 pairs: G[8q + p] holds g' of the pair (a_p, a_p + 4) of
-// word q, M[8q + p] the non-missing indicator.  The selector picks, for the high byte of each
-// half, entry c of a 4-byte table; the low bytes select a zero byte.
-//   g': 00 -> 0, 01 (missing) -> 0, 10 -> 1.0 (0x3C00), 11 -> 2.0 (0x4000)
-//   m : 00 -> 1, 01 -> 0,           10 -> 1,             11 -> 1
+__device__ __forceinline__ uint32_t relu_f16x2(uint32_t x) {
+    uint32_t y;
+    asm("fma.rn.relu.f16x2 %0, %1, %2, %3;" : "=r"(y) : "r"(x), "r"(0x3C003C00u), "r"(0u));
+    return y;
+}
+
+// 16 packed bytes = 64 codes -> FP16 pairs: M[8q + p] holds f1 of the pair (a_p, a_p + 4) of
+// word q, G[8q + p] = relu(f1) = g'.  The selector picks, for the high byte of each half, entry
+// c of a 4-byte table; the low bytes select a zero byte.
+//   f1: 00 -> 0, 01 (missing) -> -1.0 (0xBC00), 10 -> 1.0 (0x3C00), 11 -> 2.0 (0x4000)
 __device__ __forceinline__ void decode64(uint4 v, uint32_t (&G)[32], uint32_t (&M)[32]) {
-    const uint32_t TG = 0x403C0000u, TM = 0x3C3C003Cu;
+    const uint32_t TF1 = 0x403CBC00u;
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -129,8 +141,9 @@ __device__ __forceinline__ void decode64(uint4 v, uint32_t (&G)[32], uint32_t (&
 #pragma unroll
         for (int p = 0; p < 8; ++p) {
             const uint32_t sel = (sh[p] & 0x3030u) | 0x0404u;
-            G[q * 8 + p] = __byte_perm(TG, 0u, sel);
-            M[q * 8 + p] = __byte_perm(TM, 0u, sel);
+            const uint32_t f1 = __byte_perm(TF1, 0u, sel);
+            M[q * 8 + p] = f1;
+            G[q * 8 + p] = relu_f16x2(f1);
         }
     }
 }
@@ -383,11 +396,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int c = 0; c < k; ++c) {
                 float mag = 0.f;
                 if (valid) {
-                    const double y =
-                        (b * (double)acc[c * 128 + r] + a * (double)acc[(kp + c) * 128 + r]) * sc[k + c];
+                    // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum term
+                    const double y = ((b - a) * (double)acc[c * 128 + r] +
+                                      a * (double)(acc[(kp + c) * 128 + r] + args.colsumq[c])) *
+                                     sc[k + c];
                     if (args.y_out) args.y_out[(size_t)row * k + c] = y;
                     args.yt[(int64_t)c * args.yt_ld + row] = (float)y;
-                    mag = (float)(fmax(fabs(b), fabs(a)) * fabs(y));
+                    mag = (float)(fmax(fabs(b - a), fabs(a)) * fabs(y));
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
@@ -435,32 +450,46 @@ __global__ void __launch_bounds__(256) omega_scales_kernel(const double *__restr
 // individual at K position i (perm16 order inside groups of 16); zero padding elsewhere.
 __global__ void __launch_bounds__(256) omega_split_kernel(const double *__restrict__ om, int n, int k, int kp,
                                                           int n_pad, const double *__restrict__ scales,
-                                                          __half *__restrict__ out) {
+                                                          __half *__restrict__ out, long long *__restrict__ colsumq) {
     const int64_t total = (int64_t)kp * n_pad;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int c = (int)(e / n_pad), i = (int)(e - (int64_t)c * n_pad);
         const int src = (i & ~15) | perm16(i & 15);
         __half hi = __float2half(0.f), lo = __float2half(0.f);
-        if (c < k && src < n) fixed_slices(om[(size_t)src * k + c] * scales[c], hi, lo);
+        int q = 0;
+        if (c < k && src < n) {
+            const double v = om[(size_t)src * k + c] * scales[c];
+            q = (int)rint(v);
+            fixed_slices(v, hi, lo);
+        }
         out[(int64_t)c * n_pad + i] = hi;
         out[(int64_t)(kp + c) * n_pad + i] = lo;
+        // exact column sum of the quantised integers (a warp covers 32 consecutive i of one
+        // column: n_pad is a multiple of 128); integer adds, so the order does not matter
+        const int ws = __reduce_add_sync(0xffffffffu, q);
+        if ((threadIdx.x & 31) == 0 && c < k && ws != 0)
+            atomicAdd((unsigned long long *)(colsumq + c), (unsigned long long)(long long)ws);
     }
 }
 
-// Scale per column from the exact maxima, then quantise b.Y and a.Y into the X^T Y operand:
-// bop[c] = h(b.Y), bop[kp+c] = l(b.Y), bop[N+c] = h(a.Y), bop[N+kp+c] = l(a.Y), at K position s
-// the SNP perm16-ordered inside its group of 16 (zero past the last SNP).  One thread per K
-// position, all columns; the products are formed in FP32 (the scale is a power of two, so the
-// only rounding is the coefficient product's, 2^-24 relative, below the 24-bit quantisation)
-// and split in integer arithmetic: n = 4096 h + l, l in [-2048, 2047], |h| <= 2048.
+// Scale per column from the exact maxima, then quantise the X^T Y operand: bop[c], bop[kp+c] =
+// h, l of (b-a).Y (for the f2 products); bop[N+c], bop[N+kp+c] = h, l of a.Y (for f1), at K
+// position s the SNP perm16-ordered inside its group of 16 (zero past the last SNP).  The
+// quantised a.Y integers are also summed per column into rq (the rank-one term).  One thread
+// per K position, all columns; the products are formed in FP32 (the scale is a power of two,
+// so the only rounding is the coefficient product's, 2^-24 relative, below the 24-bit
+// quantisation) and split in integer arithmetic: n = 4096 h + l, l in [-2048, 2047], |h| <= 2048.
 __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict__ yt, int64_t ld, int n_snp, int k,
                                                         int kp, int N, const double *__restrict__ coef,
                                                         const unsigned int *__restrict__ colmax,
-                                                        double *__restrict__ scales, __half *__restrict__ bop) {
+                                                        double *__restrict__ scales, __half *__restrict__ bop,
+                                                        long long *__restrict__ rq) {
     __shared__ float scf[kMaxMixedNrhs];
+    __shared__ long long rqs[kMaxMixedNrhs];
     for (int c = threadIdx.x; c < k; c += blockDim.x) {
         const double sc = pow2_scale_below((double)__uint_as_float(colmax[c]) * 1.001);
         scf[c] = (float)sc;  // a power of two: exact
+        rqs[c] = 0;
         if (blockIdx.x == 0) {
             scales[2 * k + c] = sc;
             scales[3 * k + c] = 1.0 / sc;
@@ -475,23 +504,34 @@ __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict_
         const bool valid = src < n_snp;
         const float b = valid ? (float)coef[2 * (size_t)src] : 0.f;
         const float a = valid ? (float)coef[2 * (size_t)src + 1] : 0.f;
+        const float bma = b - a;
         for (int c = 0; c < k; ++c) {
             const float y = valid ? yt[(int64_t)c * ld + src] * scf[c] : 0.f;
-            const int n1 = __float2int_rn(b * y), n2 = __float2int_rn(a * y);
+            const int n1 = __float2int_rn(a * y), n2 = __float2int_rn(bma * y);
             const int h1 = (n1 + 2048) >> 12, h2 = (n2 + 2048) >> 12;
-            bop[(int64_t)c * ld + s] = __int2half_rn(h1);
-            bop[(int64_t)(kp + c) * ld + s] = __int2half_rn(n1 - (h1 << 12));
-            bop[(int64_t)(N + c) * ld + s] = __int2half_rn(h2);
-            bop[(int64_t)(N + kp + c) * ld + s] = __int2half_rn(n2 - (h2 << 12));
+            bop[(int64_t)c * ld + s] = __int2half_rn(h2);
+            bop[(int64_t)(kp + c) * ld + s] = __int2half_rn(n2 - (h2 << 12));
+            bop[(int64_t)(N + c) * ld + s] = __int2half_rn(h1);
+            bop[(int64_t)(N + kp + c) * ld + s] = __int2half_rn(n1 - (h1 << 12));
+            const int ws = __reduce_add_sync(0xffffffffu, n1);  // |n1| < 2^23: 32 of them fit
+            if ((threadIdx.x & 31) == 0 && ws != 0)
+                atomicAdd((unsigned long long *)(rqs + c), (unsigned long long)(long long)ws);
         }
     }
+    __syncthreads();
+    for (int c = threadIdx.x; c < k; c += blockDim.x)
+        if (rqs[c] != 0) atomicAdd((unsigned long long *)(rq + c), (unsigned long long)rqs[c]);
 }
 
-__global__ void reduce_parts_kernel(const double *__restrict__ partial, int64_t elems, int splits,
+// z[i][c] (+)= sum of the split partials + the rank-one term rq[c] / scale_c.
+__global__ void reduce_parts_kernel(const double *__restrict__ partial, int64_t elems, int splits, int k,
+                                    const long long *__restrict__ rq, const double *__restrict__ inv_scale,
                                     double *__restrict__ z, int accumulate) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < elems; e += (int64_t)gridDim.x * blockDim.x) {
         double s = 0.0;
         for (int p = 0; p < splits; ++p) s += partial[(int64_t)p * elems + e];
+        const int c = (int)(e % k);
+        s += (double)rq[c] * inv_scale[c];
         z[e] = accumulate ? z[e] + s : s;
     }
 }
@@ -620,7 +660,9 @@ dpca_status mixed_prepare(Handle *h) {
         (e = cudaMalloc(&m->bop, bop_elems * 2)) != cudaSuccess ||
         (e = cudaMalloc(&m->scales, 4 * (size_t)k * 8)) != cudaSuccess ||
         (e = cudaMalloc(&m->yt, (size_t)k * rows_pad * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&m->colmax, (size_t)k * 4)) != cudaSuccess) {
+        (e = cudaMalloc(&m->colmax, (size_t)k * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&m->colsumq, (size_t)k * 8)) != cudaSuccess ||
+        (e = cudaMalloc(&m->rq, (size_t)k * 8)) != cudaSuccess) {
         set_error("mixed operand allocation: %s", cudaGetErrorString(e));
         return DPCA_ERR_NOMEM;
     }
@@ -660,7 +702,7 @@ dpca_status mixed_prepare(Handle *h) {
 dpca_status mixed_release(Handle *h) {
     MixedState *m = mstate(h);
     if (!m) return DPCA_OK;
-    void *ptrs[] = {m->omega_s, m->bop, m->yt, m->colmax, m->scales, m->partial};
+    void *ptrs[] = {m->omega_s, m->bop, m->yt, m->colmax, m->scales, m->partial, m->colsumq, m->rq};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete m;
@@ -676,7 +718,9 @@ dpca_status mixed_omega_operand(Handle *h, const double *omega) {
     omega_scales_kernel<<<k, 256, 0, h->stream>>>(omega, h->n_ind, k, m->scales);
     int64_t total = (int64_t)m->kp * h->n_ind_pad;
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 8);
-    omega_split_kernel<<<grid, 256, 0, h->stream>>>(omega, h->n_ind, k, m->kp, h->n_ind_pad, m->scales, m->omega_s);
+    DPCA_CUDA(cudaMemsetAsync(m->colsumq, 0, (size_t)k * 8, h->stream));
+    omega_split_kernel<<<grid, 256, 0, h->stream>>>(omega, h->n_ind, k, m->kp, h->n_ind_pad, m->scales, m->omega_s,
+                                                    m->colsumq);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -699,9 +743,11 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     a.yt = m->yt;
     a.yt_ld = rows_pad;
     a.colmax = m->colmax;
+    a.colsumq = m->colsumq;
     a.y_out = y_out;
     a.err = h->dflag;
     DPCA_CUDA(cudaMemsetAsync(m->colmax, 0, (size_t)k * 4, h->stream));
+    DPCA_CUDA(cudaMemsetAsync(m->rq, 0, (size_t)k * 8, h->stream));
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
         mixed_gemm_kernel<kXW><<<dim3(ceil_div(rows, 128), 1), kThreads, m->smem1, h->stream>>>(map_a, m->map_om, a);
@@ -711,7 +757,7 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     const int n128 = (rows + 127) & ~127;
     int grid = std::min(ceil_div(n128, 256), h->sm_count * 8);
     bop_split_kernel<<<grid, 256, 0, h->stream>>>(m->yt, rows_pad, rows, k, m->kp, N, coef, m->colmax, m->scales,
-                                                   m->bop);
+                                                   m->bop, m->rq);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -746,7 +792,8 @@ static dpca_status xty_rows(Handle *h, const CUtensorMap &map_a, int nsnp, doubl
     ScopedLaunch t(&h->clock, h->stream, "mixed_reduce");
     int64_t elems = (int64_t)h->n_ind * k;
     int grid = (int)std::min<int64_t>((elems + 255) / 256, (int64_t)h->sm_count * 8);
-    reduce_parts_kernel<<<grid, 256, 0, h->stream>>>(m->partial, elems, splits, z, accumulate ? 1 : 0);
+    reduce_parts_kernel<<<grid, 256, 0, h->stream>>>(m->partial, elems, splits, k, m->rq, m->scales + 3 * k, z,
+                                                     accumulate ? 1 : 0);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
