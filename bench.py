@@ -229,7 +229,9 @@ def dpca_arm(a, ranks: Ranks) -> None:
     c = synth.config_cohort("incore50k", n_snp=a.n_snp, n_ind=a.n_ind)
     prec = D.PREC_MIXED if a.precision == "mixed" else D.PREC_FP64
     h = D.Handle(a.n_ind, a.n_snp, a.nrhs, precision=prec, device=dev, stream=stream.cuda_stream)
-    h.synth_fill(c)
+    h.reset_kernel_times(True)
+    h.synth_fill(c)  # the device fill, then the per-SNP decode/statistics kernel over the resident matrix
+    setup = h.kernel_times()
     omega = D.start_block(a.n_ind, a.nrhs)
     h.set_omega(omega)
     for _ in range(a.warmup):
@@ -281,11 +283,20 @@ def dpca_arm(a, ranks: Ranks) -> None:
     roof["algorithmic_per_launch"] = f"{flops:.3e} flop (2 x n_snp x n_ind x nrhs)"
     kernels = {k: {"ms_per_launch": v["ms"] / max(1, v["launches"]), "launches": v["launches"],
                    "share": v["ms"] / max(1e-9, sum(x["ms"] for x in kt.values()))} for k, v in kt.items()}
+    decode = None
+    if "snp_stats" in setup and setup["snp_stats"]["launches"]:
+        t_dec = setup["snp_stats"]["ms"] / setup["snp_stats"]["launches"] / 1e3
+        packed_bytes = a.n_snp * ((a.n_ind + 3) // 4)
+        decode = {"kernel": "snp_counts_kernel + snp_moments_kernel (decode, per-SNP counts, mean, sd, LUT)",
+                  "ms": t_dec * 1e3,
+                  "achieved_gbs": packed_bytes / t_dec / 1e9, "peak_gbs": pk["hbm_gbs"],
+                  "frac": packed_bytes / t_dec / 1e9 / pk["hbm_gbs"], "bytes_per_launch": packed_bytes,
+                  "note": "one launch per matrix (setup), timed with CUDA events on the handle's stream"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ranks.world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f16 hi+lo x exact 0/1/2, f32 accumulate, f64 dense" if a.precision ==
             "mixed" else "f64", "data": "synthetic (seeded Balding-Nichols, generated on the device)",
-            "config": workload_config(a), "clocks": clk, "gpu_launches": launches, "roofline": roof,
+            "config": workload_config(a), "clocks": clk, "gpu_launches": launches, "roofline": roof, "decode": decode,
             "kernels": kernels}
     # ---- extras (rank 0, untimed): FP64 GPU comparison, accuracy, e2e, CPU baseline ----
     host = None

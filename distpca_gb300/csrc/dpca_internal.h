@@ -76,7 +76,8 @@ struct Handle {
     double inv_sqrt_nsnp = 0;
 
     uint8_t *P = nullptr;    // SNP-major packed matrix, n_snp x pitch
-    uint8_t *PT = nullptr;   // individual-major packed matrix (mixed path), n_ind x pitchT
+    uint8_t *PT = nullptr;   // individual-major packed matrix (mixed path), pitchT bytes per individual,
+                             // stored in contiguous 128-individual x 128-byte tiles
 
     // per-SNP statistics
     int32_t *counts = nullptr;  // [n_snp][4] codes 00,01,10,11
@@ -107,7 +108,7 @@ struct Handle {
     const uint8_t *hostP = nullptr;   // caller-owned host rows, host_stride bytes apart
     int64_t host_stride = 0;
     uint8_t *Pb[2] = {nullptr, nullptr};   // block buffers, blk x pitch
-    uint8_t *PTb[2] = {nullptr, nullptr};  // mixed: block transposes, n_ind x pitchTb
+    uint8_t *PTb[2] = {nullptr, nullptr};  // mixed: block transposes, pitchTb per individual, tiled as PT
     int64_t pitchTb = 0;
     uint8_t *Sb[2] = {nullptr, nullptr};   // staging for one contiguous host copy per block (host rows
                                            // whose stride is not the device pitch), re-pitched on device

@@ -171,8 +171,8 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
             DPCA_TRY(dalloc(&h->Pb[b], (size_t)h->blk * h->pitch));
             DPCA_CUDA(cudaMemsetAsync(h->Pb[b], 0, (size_t)h->blk * h->pitch, h->stream));
             if (precision == DPCA_PREC_MIXED) {
-                DPCA_TRY(dalloc(&h->PTb[b], (size_t)n_ind * h->pitchTb));
-                DPCA_CUDA(cudaMemsetAsync(h->PTb[b], 0, (size_t)n_ind * h->pitchTb, h->stream));
+                DPCA_TRY(dalloc(&h->PTb[b], round_up((size_t)n_ind, 128) * h->pitchTb));
+                DPCA_CUDA(cudaMemsetAsync(h->PTb[b], 0, round_up((size_t)n_ind, 128) * h->pitchTb, h->stream));
             }
             DPCA_CUDA(cudaEventCreateWithFlags(&h->copied[b], cudaEventDisableTiming));
             DPCA_CUDA(cudaEventCreateWithFlags(&h->consumed[b], cudaEventDisableTiming));
@@ -212,8 +212,9 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
     DPCA_CUDA(cudaMallocHost((void **)&h->host_small, L.total() * sizeof(double)));
     if (precision == DPCA_PREC_MIXED) {
         if (!h->streamed) {
-            DPCA_TRY(dalloc(&h->PT, (size_t)n_ind * h->pitchT));
-            DPCA_CUDA(cudaMemsetAsync(h->PT, 0, (size_t)n_ind * h->pitchT, h->stream));
+            // tile-blocked (see transpose_packed_kernel): rows padded to whole 128-row tiles
+            DPCA_TRY(dalloc(&h->PT, round_up((size_t)n_ind, 128) * h->pitchT));
+            DPCA_CUDA(cudaMemsetAsync(h->PT, 0, round_up((size_t)n_ind, 128) * h->pitchT, h->stream));
         }
         DPCA_TRY(mixed_prepare(h));
     }

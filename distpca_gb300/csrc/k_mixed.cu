@@ -85,6 +85,7 @@ struct GemmArgs {
     int kb_per_split;  // K blocks per CTA (multiple of 8)
     int k, kp, N;
     int ring;          // batches in flight (B stages in shared memory)
+    int a_ktiles;      // kXTY: 128-byte K tiles per 128-row tile of the tile-blocked A operand
     const double *coef;     // kXW: [rows][2] {b, a}
     const double *scales;   // [4][k]: omega scale, its inverse, b/aY scale, its inverse
     float *yt;              // kXW: Y transposed, [k][yt_ld] (FP32)
@@ -250,7 +251,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if ((t & 3) == 0) {
                     if (!tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true)) break;
                     tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
-                    tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (kb0 + 2 * t) * 16, tile * 128);
+                    if (MODE == kXTY)  // tile-blocked: tile (row block, K tile) at row ((rb * nkt) + kt) * 128
+                        tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], 0,
+                                        (tile * args.a_ktiles + ((kb0 + 2 * t) >> 3)) * 128);
+                    else
+                        tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (kb0 + 2 * t) * 16, tile * 128);
                     issued_p = (t >> 2) + 1;
                     if (++sp == kPStages) sp = 0, pph ^= 1;
                 }
@@ -681,14 +686,14 @@ dpca_status mixed_prepare(Handle *h) {
     m->smem2 = smem_bytes(kXTY, N, m->kp, m->ring2);
     if (!h->streamed) {
         DPCA_TRY(make_map(&m->map_p[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->P, h->pitch, h->n_snp, h->pitch, 128, 128));
-        DPCA_TRY(make_map(&m->map_pt[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PT, h->pitchT, h->n_ind, h->pitchT, 128,
-                          128));
+        DPCA_TRY(make_map(&m->map_pt[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PT, 128,
+                          (uint64_t)(h->n_ind + 127) / 128 * h->pitchT, 128, 128, 128));
     } else {
         for (int b = 0; b < 2; ++b) {
             DPCA_TRY(make_map(&m->map_p[b], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->Pb[b], h->pitch, h->blk, h->pitch, 128,
                               128));
-            DPCA_TRY(make_map(&m->map_pt[b], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PTb[b], h->pitchTb, h->n_ind,
-                              h->pitchTb, 128, 128));
+            DPCA_TRY(make_map(&m->map_pt[b], CU_TENSOR_MAP_DATA_TYPE_UINT8, h->PTb[b], 128,
+                              (uint64_t)(h->n_ind + 127) / 128 * h->pitchTb, 128, 128, 128));
         }
     }
     DPCA_TRY(make_batch_map(&m->map_om, m->omega_s, h->n_ind_pad, N));
@@ -774,6 +779,7 @@ static dpca_status xty_rows(Handle *h, const CUtensorMap &map_a, int nsnp, doubl
     }
     GemmArgs a{};
     a.rows = h->n_ind;
+    a.a_ktiles = (int)((h->streamed ? h->pitchTb : h->pitchT) / 128);
     a.nkb_total = ceil_div(nsnp, 64);
     a.kb_per_split = kb_per_split;
     a.k = k;

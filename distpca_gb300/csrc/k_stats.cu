@@ -1,88 +1,106 @@
 // Per-SNP decode statistics, the synthetic-cohort fill, and the individual-major
 // transposed copy of the packed matrix.
 //
-// snp_stats_kernel restates, on the device and bit-exactly,
+// snp_counts_kernel + snp_moments_kernel restate, on the device and bit-exactly,
 //   decode_plink_sse2 (utilities.cpp:351-414): code 00 -> 0, 01 -> missing, 10 -> 1, 11 -> 2;
 //   standardize (utilities.cpp:272-292): avg = sum/ctr over non-missing, p = avg/2,
 //     sd = sqrt(2p(1-p)) -- all in IEEE FP64 with explicit round-to-nearest ops so that no
 //     contraction can change a bit;
 //   the LUT cache (methods.cpp:819-843): value per code = ((g - avg)/sd) * (1/sqrt(n_snp)),
 //     zero for missing codes and for SNPs with sd <= 1e-9.
-// Counting is a popcount over 16 codes per 32-bit word with 128-bit coalesced loads; one warp
-// owns one SNP row and reduces its four counts with shuffles.
+// The streaming pass (counts) is separate from the per-SNP FP64 arithmetic (moments), so that
+// the divisions and square roots stay off the HBM-bound loop: one warp streams one SNP row with
+// 128-bit coalesced loads and three population counts per pair of words, reduced with shuffles.
+#include <algorithm>
+
 #include "common.cuh"
 #include "dpca_internal.h"
 
 namespace dpca {
 
-__global__ void __launch_bounds__(256) snp_stats_kernel(const uint8_t *__restrict__ P, int64_t pitch, int n_ind,
-                                                        int n_snp, int64_t np, double inv_sqrt_nsnp,
-                                                        int32_t *__restrict__ counts, double *__restrict__ avg,
-                                                        double *__restrict__ sd, double *__restrict__ lut,
-                                                        double *__restrict__ coef) {
+// Pass 1: counts only.  One warp per SNP row streams the row with 16-byte loads; per pair of
+// words three population counts give popc(hi) = c10 + c11, popc(lo) = c01 + c11 and
+// popc(hi & lo) = c11 (two words' even-position bits interleaved into one word).
+__global__ void __launch_bounds__(256) snp_counts_kernel(const uint8_t *__restrict__ P, int64_t pitch, int n_ind,
+                                                         int n_snp, int64_t np, int32_t *__restrict__ counts) {
     int lane = threadIdx.x & 31;
     int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (s >= n_snp) return;
     const uint4 *row = reinterpret_cast<const uint4 *>(P + s * pitch);
     int nchunk = (int)((np + 15) >> 4);
-    int c00 = 0, c01 = 0, c10 = 0, c11 = 0;
-#pragma unroll 4
+    int n_hi = 0, n_lo = 0, n_11 = 0, n_valid = 0;
+#pragma unroll 8
     for (int c = lane; c < nchunk; c += 32) {
         uint4 v = __ldg(row + c);
         uint32_t ws[4] = {v.x, v.y, v.z, v.w};
+        uint32_t hi[4], lo[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             int base = c * 64 + j * 16;  // first individual of this word
             int valid = n_ind - base;
             uint32_t m = valid >= 16 ? 0x55555555u : (valid <= 0 ? 0u : (((1u << (2 * valid)) - 1u) & 0x55555555u));
-            uint32_t hi = (ws[j] >> 1) & m, lo = ws[j] & m;
-            c11 += __popc(hi & lo);
-            c10 += __popc(hi & ~lo);
-            c01 += __popc(~hi & lo);
-            c00 += __popc(m & ~hi & ~lo);
+            hi[j] = (ws[j] >> 1) & m;
+            lo[j] = ws[j] & m;
+            n_valid += valid >= 16 ? 16 : (valid <= 0 ? 0 : valid);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j += 2) {
+            const uint32_t h2 = hi[j] | (hi[j + 1] << 1), l2 = lo[j] | (lo[j + 1] << 1);
+            n_hi += __popc(h2);
+            n_lo += __popc(l2);
+            n_11 += __popc(h2 & l2);
         }
     }
-    c00 = warp_sum_int(c00);
-    c01 = warp_sum_int(c01);
-    c10 = warp_sum_int(c10);
-    c11 = warp_sum_int(c11);
+    n_hi = warp_sum_int(n_hi);
+    n_lo = warp_sum_int(n_lo);
+    n_11 = warp_sum_int(n_11);
+    n_valid = warp_sum_int(n_valid);
     if (lane != 0) return;
+    const int c11 = n_11, c10 = n_hi - n_11, c01 = n_lo - n_11, c00 = n_valid - c01 - c10 - c11;
     counts[4 * s + 0] = c00;
     counts[4 * s + 1] = c01;
     counts[4 * s + 2] = c10;
     counts[4 * s + 3] = c11;
-    double sum = (double)c10 + 2.0 * (double)c11;  // exact: small integers
-    unsigned int ctr = (unsigned int)(c00 + c10 + c11);
-    double mean = __ddiv_rn(sum, (double)ctr);
-    double p = __ddiv_rn(mean, 2.0);
-    double sdev = __dsqrt_rn(__dmul_rn(__dmul_rn(2.0, p), __dsub_rn(1.0, p)));
-    avg[s] = mean;
-    sd[s] = sdev;
-    double v00 = 0.0, v10 = 0.0, v11 = 0.0, b = 0.0, a = 0.0;
-    if (sdev > 1e-9) {
-        v00 = __dmul_rn(__ddiv_rn(__dsub_rn(0.0, mean), sdev), inv_sqrt_nsnp);
-        v10 = __dmul_rn(__ddiv_rn(__dsub_rn(1.0, mean), sdev), inv_sqrt_nsnp);
-        v11 = __dmul_rn(__ddiv_rn(__dsub_rn(2.0, mean), sdev), inv_sqrt_nsnp);
-        b = inv_sqrt_nsnp / sdev;
-        a = -mean * b;
-    }
-    lut[4 * s + 0] = v00;
-    lut[4 * s + 1] = 0.0;
-    lut[4 * s + 2] = v10;
-    lut[4 * s + 3] = v11;
-    if (coef) {
-        coef[2 * s + 0] = b;
-        coef[2 * s + 1] = a;
+}
+
+// Pass 2: one thread per SNP turns its counts into mean, sd, the LUT and the mixed-path
+// coefficients (the FP64 divisions stay off the streaming pass).
+__global__ void __launch_bounds__(256) snp_moments_kernel(int n_snp, double inv_sqrt_nsnp,
+                                                          const int32_t *__restrict__ counts, double *__restrict__ avg,
+                                                          double *__restrict__ sd, double *__restrict__ lut,
+                                                          double *__restrict__ coef) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_snp; s += (int64_t)gridDim.x * blockDim.x) {
+        const int c00 = counts[4 * s + 0], c10 = counts[4 * s + 2], c11 = counts[4 * s + 3];
+        double sum = (double)c10 + 2.0 * (double)c11;  // exact: small integers
+        unsigned int ctr = (unsigned int)(c00 + c10 + c11);
+        double mean = __ddiv_rn(sum, (double)ctr);
+        double p = __ddiv_rn(mean, 2.0);
+        double sdev = __dsqrt_rn(__dmul_rn(__dmul_rn(2.0, p), __dsub_rn(1.0, p)));
+        avg[s] = mean;
+        sd[s] = sdev;
+        double v00 = 0.0, v10 = 0.0, v11 = 0.0, b = 0.0, a = 0.0;
+        if (sdev > 1e-9) {
+            v00 = __dmul_rn(__ddiv_rn(__dsub_rn(0.0, mean), sdev), inv_sqrt_nsnp);
+            v10 = __dmul_rn(__ddiv_rn(__dsub_rn(1.0, mean), sdev), inv_sqrt_nsnp);
+            v11 = __dmul_rn(__ddiv_rn(__dsub_rn(2.0, mean), sdev), inv_sqrt_nsnp);
+            b = inv_sqrt_nsnp / sdev;
+            a = -mean * b;
+        }
+        lut[4 * s + 0] = v00;
+        lut[4 * s + 1] = 0.0;
+        lut[4 * s + 2] = v10;
+        lut[4 * s + 3] = v11;
+        if (coef) {
+            coef[2 * s + 0] = b;
+            coef[2 * s + 1] = a;
+        }
     }
 }
 
 dpca_status launch_snp_stats(Handle *h) {
     ScopedLaunch t(&h->clock, h->stream, "snp_stats");
-    int warps_per_block = 8;
-    int grid = ceil_div(h->n_snp, warps_per_block);
-    snp_stats_kernel<<<grid, 32 * warps_per_block, 0, h->stream>>>(h->P, h->pitch, h->n_ind, h->n_snp, h->np,
-                                                                     h->inv_sqrt_nsnp, h->counts, h->avg, h->sd,
-                                                                     h->lut, h->coef);
+    launch_snp_stats_raw(h->P, h->pitch, h->n_ind, h->n_snp, h->inv_sqrt_nsnp, h->counts, h->avg, h->sd, h->lut,
+                         h->coef, h->stream);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -93,8 +111,9 @@ dpca_status launch_snp_stats(Handle *h) {
 void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, double inv_sqrt_nsnp,
                           int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream) {
     const int64_t np = ((int64_t)n_ind + 3) / 4;
-    snp_stats_kernel<<<ceil_div(n_snp, 8), 256, 0, stream>>>(P, pitch, n_ind, n_snp, np, inv_sqrt_nsnp, counts, avg,
-                                                            sd, lut, coef);
+    snp_counts_kernel<<<ceil_div(n_snp, 8), 256, 0, stream>>>(P, pitch, n_ind, n_snp, np, counts);
+    snp_moments_kernel<<<std::min(ceil_div(n_snp, 256), 4096), 256, 0, stream>>>(n_snp, inv_sqrt_nsnp, counts, avg,
+                                                                                  sd, lut, coef);
 }
 
 // One thread writes one 32-bit word (16 individuals) of one SNP row; the
@@ -182,8 +201,12 @@ __global__ void __launch_bounds__(256) transpose_packed_kernel(const uint8_t *__
             }
             out[j] = w;
         }
-        int64_t byte0 = (int64_t)(s0 >> 2);
-        *reinterpret_cast<uint4 *>(PT + (int64_t)i * pitchT + byte0) = make_uint4(out[0], out[1], out[2], out[3]);
+        // tile-blocked layout: 128 individuals x 128 bytes (512 SNPs) per contiguous 16 KB tile,
+        // tiles of one row block consecutive along the SNPs, so that a TMA tile load touches one
+        // contiguous range instead of 128 rows a whole matrix row apart
+        const int64_t byte0 = (int64_t)(s0 >> 2), nkt = pitchT / 128;
+        uint8_t *dst = PT + (((int64_t)(i >> 7) * nkt + (byte0 >> 7)) * 128 + (i & 127)) * 128 + (byte0 & 127);
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(out[0], out[1], out[2], out[3]);
     }
 }
 
