@@ -110,6 +110,7 @@ struct Handle {
     uint8_t *Pb[2] = {nullptr, nullptr};   // block buffers, blk x pitch
     uint8_t *PTb[2] = {nullptr, nullptr};  // mixed: block transposes, pitchTb per individual, tiled as PT
     int64_t pitchTb = 0;
+    size_t sb_bytes = 0;
     uint8_t *Sb[2] = {nullptr, nullptr};   // staging for one contiguous host copy per block (host rows
                                            // whose stride is not the device pitch), re-pitched on device
     cudaStream_t cstream = nullptr;        // copy stream
@@ -140,7 +141,7 @@ dpca_status launch_transpose_packed(Handle *h);
 void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, double inv_sqrt_nsnp,
                           int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream);
 void launch_transpose_raw(const uint8_t *P, int64_t pitch, uint8_t *PT, int64_t pitchT, int n_ind, int n_snp,
-                          cudaStream_t stream);
+                          cudaStream_t stream, int s_base = 0);
 // one streamed block: Z (+)= X_b^T (X_b Omega) over SNP rows [s0, s0 + ns) held in buffer b
 dpca_status launch_fp64_block(Handle *h, int b, int s0, int ns, const double *omega, double *z, bool accumulate);
 dpca_status mixed_omega_operand(Handle *h, const double *omega);

@@ -449,6 +449,64 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     return DPCA_OK;
 }
 
+// Resident upload, pipelined in chunks of whole 512-SNP tiles: each chunk's rows are copied
+// contiguously (full host-link speed; a row-pitched copy of .bed-layout rows ran ~25% slower)
+// into a staging buffer on a copy stream, re-pitched into P on the device, and its per-SNP
+// statistics and transposed tiles computed while the next chunk is copied.
+static dpca_status upload_pipelined(Handle *h, const uint8_t *packed, int64_t row_stride) {
+    ScopedLaunch t(&h->clock, h->stream, "h2d_packed");
+    int64_t rows_per = std::max<int64_t>(512, ((int64_t)(256 << 20) / std::max<int64_t>(1, row_stride)) / 512 * 512);
+    rows_per = std::min<int64_t>(rows_per, ((int64_t)h->n_snp + 511) / 512 * 512);
+    const bool direct = row_stride == h->pitch;  // rows already at the device pitch
+    dpca_status st = DPCA_OK;
+    auto check = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == DPCA_OK) {
+            set_error("upload: %s: %s", what, cudaGetErrorString(e));
+            st = e == cudaErrorMemoryAllocation ? DPCA_ERR_NOMEM : DPCA_ERR_CUDA;
+        }
+        return st == DPCA_OK;
+    };
+    // copy stream, events and staging buffers are kept by the handle (freed with it)
+    if (!h->cstream) check(cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking), "stream");
+    for (int b = 0; b < 2 && st == DPCA_OK; ++b) {
+        if (!h->copied[b]) check(cudaEventCreateWithFlags(&h->copied[b], cudaEventDisableTiming), "event");
+        if (!h->consumed[b]) check(cudaEventCreateWithFlags(&h->consumed[b], cudaEventDisableTiming), "event");
+        if (!direct && (!h->Sb[b] || h->sb_bytes < (size_t)rows_per * row_stride)) {
+            if (h->Sb[b]) cudaFree(h->Sb[b]);
+            h->Sb[b] = nullptr;
+            check(cudaMalloc(&h->Sb[b], (size_t)rows_per * row_stride), "staging");
+        }
+    }
+    if (!direct && st == DPCA_OK) h->sb_bytes = (size_t)rows_per * row_stride;
+    cudaStream_t cs = h->cstream;
+    uint8_t **stage = h->Sb;
+    cudaEvent_t *copied = h->copied, *freed = h->consumed;
+    for (int64_t s0 = 0, j = 0; s0 < h->n_snp && st == DPCA_OK; s0 += rows_per, ++j) {
+        const int b = (int)(j & 1);
+        const int rows = (int)std::min<int64_t>(rows_per, h->n_snp - s0);
+        const uint8_t *src = packed + s0 * row_stride;
+        uint8_t *dst = h->P + s0 * h->pitch;
+        check(cudaStreamWaitEvent(cs, freed[b], 0), "wait");
+        if (direct)
+            check(cudaMemcpyAsync(dst, src, (size_t)rows * row_stride, cudaMemcpyHostToDevice, cs), "copy");
+        else
+            check(cudaMemcpyAsync(stage[b], src, (size_t)rows * row_stride, cudaMemcpyHostToDevice, cs), "copy");
+        check(cudaEventRecord(copied[b], cs), "record");
+        check(cudaStreamWaitEvent(h->stream, copied[b], 0), "wait");
+        if (!direct)
+            check(cudaMemcpy2DAsync(dst, h->pitch, stage[b], row_stride, h->np, rows, cudaMemcpyDeviceToDevice,
+                                    h->stream),
+                  "re-pitch");
+        check(cudaEventRecord(freed[b], h->stream), "record");
+        launch_snp_stats_raw(dst, h->pitch, h->n_ind, rows, h->inv_sqrt_nsnp, h->counts + 4 * s0, h->avg + s0,
+                             h->sd + s0, h->lut + 4 * s0, h->coef + 2 * s0, h->stream);
+        if (h->precision == DPCA_PREC_MIXED)
+            launch_transpose_raw(dst, h->pitch, h->PT, h->pitchT, h->n_ind, rows, h->stream, (int)s0);
+        check(cudaGetLastError(), "launch");
+    }
+    return st;
+}
+
 }  // namespace dpca
 
 using namespace dpca;
@@ -519,24 +577,17 @@ dpca_status dpca_upload(dpca_handle *hh, const uint8_t *packed, int64_t row_stri
                 if (h->Sb[b]) cudaFree(h->Sb[b]);
                 h->Sb[b] = nullptr;
                 DPCA_TRY(dalloc(&h->Sb[b], (size_t)h->blk * row_stride));
+                h->sb_bytes = (size_t)h->blk * row_stride;
             }
         }
         DPCA_TRY(after_data(h));
         return DPCA_OK;
     }
-    {
-        ScopedLaunch t(&h->clock, h->stream, "h2d_packed");
-        // chunked 2D copies keep each transfer bounded
-        const int64_t rows_per = std::max<int64_t>(1, (int64_t)(256 << 20) / std::max<int64_t>(1, row_stride));
-        for (int64_t s0 = 0; s0 < h->n_snp; s0 += rows_per) {
-            int64_t rows = std::min<int64_t>(rows_per, h->n_snp - s0);
-            DPCA_CUDA(cudaMemcpy2DAsync(h->P + s0 * h->pitch, h->pitch, packed + s0 * row_stride, row_stride, h->np,
-                                        rows, cudaMemcpyHostToDevice, h->stream));
-        }
-    }
-    DPCA_TRY(after_data(h));
+    DPCA_TRY(upload_pipelined(h, packed, row_stride));
+    h->stats_ready = true;
     return DPCA_OK;
 }
+
 
 dpca_status dpca_synth_fill(dpca_handle *hh, uint64_t key, const uint8_t *pop, const uint32_t *miss_thr,
                             const uint32_t *snp_thr, int n_pop) {

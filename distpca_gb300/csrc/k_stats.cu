@@ -168,7 +168,7 @@ constexpr int kTI = 256;  // individuals per tile
 
 __global__ void __launch_bounds__(256) transpose_packed_kernel(const uint8_t *__restrict__ P, int64_t pitch,
                                                                uint8_t *__restrict__ PT, int64_t pitchT, int n_ind,
-                                                               int n_snp) {
+                                                               int n_snp, int s_base) {
     __shared__ uint8_t codes[kTS][kTI + 4];
     int s0 = blockIdx.y * kTS, i0 = blockIdx.x * kTI;
     int tid = threadIdx.x;
@@ -204,22 +204,23 @@ __global__ void __launch_bounds__(256) transpose_packed_kernel(const uint8_t *__
         // tile-blocked layout: 128 individuals x 128 bytes (512 SNPs) per contiguous 16 KB tile,
         // tiles of one row block consecutive along the SNPs, so that a TMA tile load touches one
         // contiguous range instead of 128 rows a whole matrix row apart
-        const int64_t byte0 = (int64_t)(s0 >> 2), nkt = pitchT / 128;
+        const int64_t byte0 = (int64_t)((s0 + s_base) >> 2), nkt = pitchT / 128;
         uint8_t *dst = PT + (((int64_t)(i >> 7) * nkt + (byte0 >> 7)) * 128 + (i & 127)) * 128 + (byte0 & 127);
         *reinterpret_cast<uint4 *>(dst) = make_uint4(out[0], out[1], out[2], out[3]);
     }
 }
 
+// Rows [0, n_snp) of P are SNPs s_base + [0, n_snp) of PT (s_base a multiple of 64).
 void launch_transpose_raw(const uint8_t *P, int64_t pitch, uint8_t *PT, int64_t pitchT, int n_ind, int n_snp,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, int s_base) {
     dim3 grid(ceil_div(n_ind, kTI), ceil_div(n_snp, kTS));
-    transpose_packed_kernel<<<grid, 256, 0, stream>>>(P, pitch, PT, pitchT, n_ind, n_snp);
+    transpose_packed_kernel<<<grid, 256, 0, stream>>>(P, pitch, PT, pitchT, n_ind, n_snp, s_base);
 }
 
 dpca_status launch_transpose_packed(Handle *h) {
     ScopedLaunch t(&h->clock, h->stream, "transpose_packed");
     dim3 grid(ceil_div(h->n_ind, kTI), ceil_div(h->n_snp, kTS));
-    transpose_packed_kernel<<<grid, 256, 0, h->stream>>>(h->P, h->pitch, h->PT, h->pitchT, h->n_ind, h->n_snp);
+    transpose_packed_kernel<<<grid, 256, 0, h->stream>>>(h->P, h->pitch, h->PT, h->pitchT, h->n_ind, h->n_snp, 0);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
