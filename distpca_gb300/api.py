@@ -17,7 +17,7 @@ import numpy as np
 
 __all__ = ["DpcaError", "Config", "Result", "Handle", "lib", "library_path", "config", "parse_args", "probe",
            "resolve", "start_block", "run", "run_packed", "decode_counts", "PREC_FP64", "PREC_MIXED",
-           "exported_symbols", "FullSVD", "full_svd"]
+           "exported_symbols", "FullSVD", "full_svd", "Server", "JobInfo"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PREC_FP64 = 0
@@ -59,6 +59,23 @@ class Result(ctypes.Structure):
 
 def library_path() -> str:
     return os.environ.get("DPCA_LIBRARY", os.path.join(HERE, "_build", "libdpca.so"))
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("slots", ctypes.c_int), ("hbm_budget_gb", ctypes.c_double)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("n_ind", ctypes.c_int), ("n_snp", ctypes.c_int), ("cfg", Config), ("packed", ctypes.c_void_p),
+                ("row_stride", ctypes.c_int64), ("synth_key", ctypes.c_uint64), ("synth_pop", ctypes.c_void_p),
+                ("synth_miss_thr", ctypes.c_void_p), ("synth_snp_thr", ctypes.c_void_p), ("synth_n_pop", ctypes.c_int),
+                ("omega", ctypes.c_void_p), ("sigma", ctypes.c_void_p), ("u", ctypes.c_void_p)]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("total_its", ctypes.c_int), ("passes", ctypes.c_int),
+                ("t_submit", ctypes.c_double), ("t_start", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("device_gb", ctypes.c_double), ("error", ctypes.c_char * 256)]
 
 
 _lib = None
@@ -106,6 +123,14 @@ _SIGS = {
                                           ctypes.c_void_p]),
     "dpca_decode_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dpca_serve_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ServeConfig)]),
+    "dpca_serve_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_int64)]),
+    "dpca_serve_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(JobInfo)]),
+    "dpca_serve_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.POINTER(JobInfo)]),
+    "dpca_serve_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "dpca_serve_shutdown": (ctypes.c_int, [ctypes.c_void_p]),
 }
 
 
@@ -386,3 +411,93 @@ def full_svd(result: Dict, n_ind: int, n_snp: int, packed: Optional[np.ndarray] 
     out["vec_relerr"] = out["vec_relerr"].reshape(n_ind, nsv)
     out.update(info=f.info, time_true_svd=f.time_true_svd, frob_norm_angle=f.frob_norm_angle, cos_error=f.cos_error)
     return out
+
+
+class Server:
+    """The serving loop (dpca_serve_*): independent PCA jobs, up to `slots` in flight on one GPU.
+
+    submit() takes packed host rows or a synthetic cohort (distpca_gb300.synth.Cohort) and the
+    run flags; it returns a job id at once.  The arrays a job reads and writes are kept referenced
+    here until the job has been waited for.  result(job) waits and returns the job's
+    {"sigma", "u", "its", "passes", "info"}.
+    """
+
+    def __init__(self, device: int = 0, slots: int = 4, hbm_gb: float = 0.0):
+        c = ServeConfig(device, slots, hbm_gb)
+        s = ctypes.c_void_p()
+        _check(lib().dpca_serve_create(ctypes.byref(s), ctypes.byref(c)))
+        self._s = s
+        self._keep: Dict[int, tuple] = {}
+
+    def submit(self, n_ind: int, n_snp: int, packed: Optional[np.ndarray] = None, cohort=None,
+               omega0: Optional[np.ndarray] = None, want_u: bool = True, **flags) -> int:
+        c = config(**flags)
+        j = Job()
+        j.n_ind, j.n_snp, j.cfg = n_ind, n_snp, c
+        keep = []
+        if packed is not None:
+            packed = np.ascontiguousarray(packed, dtype=np.uint8)
+            assert packed.shape[0] == n_snp
+            j.packed, j.row_stride = packed.ctypes.data, packed.shape[1]
+            keep.append(packed)
+        else:
+            pop = np.ascontiguousarray(cohort.pop, dtype=np.uint8)
+            miss = np.ascontiguousarray(cohort.miss_thr, dtype=np.uint32)
+            thr = np.ascontiguousarray(cohort.snp_thr, dtype=np.uint32)
+            j.synth_key, j.synth_n_pop = cohort.key, cohort.n_pop
+            j.synth_pop, j.synth_miss_thr, j.synth_snp_thr = pop.ctypes.data, miss.ctypes.data, thr.ctypes.data
+            keep += [pop, miss, thr]
+        if omega0 is not None:
+            omega0 = np.ascontiguousarray(omega0, dtype=np.float64)
+            assert omega0.shape == (n_ind, c.nrhs)
+            j.omega = omega0.ctypes.data
+            keep.append(omega0)
+        sigma = np.zeros(c.nsv)
+        u = np.zeros((n_ind, c.nsv)) if want_u else None
+        j.sigma = sigma.ctypes.data
+        j.u = u.ctypes.data if u is not None else None
+        jid = ctypes.c_int64(0)
+        _check(lib().dpca_serve_submit(self._s, ctypes.byref(j), ctypes.byref(jid)))
+        self._keep[jid.value] = (keep, sigma, u)
+        return jid.value
+
+    def poll(self, job: int) -> bool:
+        done = ctypes.c_int(0)
+        _check(lib().dpca_serve_poll(self._s, job, ctypes.byref(done), None))
+        return bool(done.value)
+
+    def wait(self, job: int, timeout: float = -1.0) -> JobInfo:
+        info = JobInfo()
+        _check(lib().dpca_serve_wait(self._s, job, timeout, ctypes.byref(info)))
+        return info
+
+    def result(self, job: int, timeout: float = -1.0) -> Dict:
+        info = self.wait(job, timeout)
+        keep, sigma, u = self._keep.pop(job)
+        if info.status != 0:
+            raise DpcaError(info.status, info.error.decode(errors="replace"))
+        return {"sigma": sigma, "u": u, "its": info.total_its, "passes": info.passes, "info": info}
+
+    def stats(self) -> Dict:
+        done, mif, peak, budget = ctypes.c_int64(0), ctypes.c_int(0), ctypes.c_double(0), ctypes.c_double(0)
+        _check(lib().dpca_serve_stats(self._s, ctypes.byref(done), ctypes.byref(mif), ctypes.byref(peak),
+                                      ctypes.byref(budget)))
+        return {"done": done.value, "max_in_flight": mif.value, "peak_gb": peak.value, "budget_gb": budget.value}
+
+    def shutdown(self) -> None:
+        if self._s:
+            lib().dpca_serve_shutdown(self._s)
+            self._s = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.shutdown()
+
+    def __del__(self):
+        try:
+            self.shutdown()
+        except Exception:
+            pass

@@ -116,8 +116,33 @@ struct Handle {
     cudaStream_t cstream = nullptr;        // copy stream
     cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
 
+    // Device allocations: cudaMalloc, or stream-ordered on `stream` (cudaMallocAsync / cudaFreeAsync)
+    // for handles of the serving loop, so that creating and freeing one job's buffers never
+    // synchronises the device under the other jobs' work.  dev_bytes counts what is held.
+    bool async_alloc = false;
+    size_t dev_bytes = 0;
+    // Most blocks of a cooperative (grid-synchronising) launch, 0 = one per SM.  Handles of the
+    // serving loop get sm_count / slots, so that the cooperative grids of all jobs in flight fit
+    // the GPU together: none can wait on blocks that another job's spinning grid keeps out.
+    int coop_blocks = 0;
+
     KernelClock clock;
 };
+
+// Raise a kernel's dynamic shared-memory limit to the current device's opt-in maximum, once
+// per (kernel, device).  The limit is a process-wide function attribute: setting it to each
+// launch's own size races between host threads that launch the same kernel with different
+// sizes (the serving loop's workers), so it is set once, to the largest value.
+dpca_status allow_max_smem(const void *func);
+
+dpca_status dev_alloc(Handle *h, void **p, size_t bytes);
+void dev_free(Handle *h, void *p);
+// Device bytes a resident handle of these sizes holds (what create_impl and mixed_prepare allocate).
+size_t handle_footprint(int n_ind, int n_snp, int nrhs, int precision, int sm_count);
+size_t mixed_footprint(int n_ind, int n_snp, int nrhs, int sm_count);
+// Resident handle for the serving loop: stream-ordered allocations on `stream`, pageable result mirror.
+dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device,
+                                  cudaStream_t stream, int coop_blocks);
 
 // Offsets (in doubles) inside Handle::small.
 struct SmallLayout {

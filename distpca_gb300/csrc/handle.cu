@@ -9,6 +9,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <set>
 
 #include "common.cuh"
 #include "dpca_internal.h"
@@ -83,17 +85,48 @@ bool env_flag(const char *name) {
 
 static size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
 
-template <typename T>
-static dpca_status dalloc(T **p, size_t elems) {
+dpca_status allow_max_smem(const void *func) {
+    static std::mutex mu;
+    static std::set<std::pair<const void *, int>> done;
+    int dev = 0;
+    DPCA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({func, dev})) return DPCA_OK;
+    int optin = 0;
+    DPCA_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa{};
+    DPCA_CUDA(cudaFuncGetAttributes(&fa, func));
+    DPCA_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   optin - (int)fa.sharedSizeBytes));
+    done.insert({func, dev});
+    return DPCA_OK;
+}
+
+dpca_status dev_alloc(Handle *h, void **p, size_t bytes) {
     *p = nullptr;
-    if (elems == 0) return DPCA_OK;
-    cudaError_t e = cudaMalloc((void **)p, elems * sizeof(T));
+    if (bytes == 0) return DPCA_OK;
+    cudaError_t e = h->async_alloc ? cudaMallocAsync(p, bytes, h->stream) : cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
-        set_error("cudaMalloc(%zu bytes): %s", elems * sizeof(T), cudaGetErrorString(e));
+        cudaGetLastError();
+        set_error("device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
         *p = nullptr;
         return DPCA_ERR_NOMEM;
     }
+    h->dev_bytes += bytes;
     return DPCA_OK;
+}
+
+void dev_free(Handle *h, void *p) {
+    if (!p) return;
+    if (h->async_alloc)
+        cudaFreeAsync(p, h->stream);
+    else
+        cudaFree(p);
+}
+
+template <typename T>
+static dpca_status dalloc(Handle *h, T **p, size_t elems) {
+    return dev_alloc(h, (void **)p, elems * sizeof(T));
 }
 
 static void free_all(Handle *h) {
@@ -102,14 +135,18 @@ static void free_all(Handle *h) {
                     h->omega, h->z,     h->q,      h->old,      h->work, h->y,     h->partial,
                     h->small, h->red,   h->dflag,  h->Pb[0],    h->Pb[1], h->PTb[0], h->PTb[1],
                     h->Sb[0], h->Sb[1]};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    for (void *p : ptrs) dev_free(h, p);
     for (int b = 0; b < 2; ++b) {
         if (h->copied[b]) cudaEventDestroy(h->copied[b]);
         if (h->consumed[b]) cudaEventDestroy(h->consumed[b]);
     }
     if (h->cstream) cudaStreamDestroy(h->cstream);
-    if (h->host_small) cudaFreeHost(h->host_small);
+    if (h->host_small) {
+        if (h->async_alloc)
+            free(h->host_small);
+        else
+            cudaFreeHost(h->host_small);
+    }
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -168,57 +205,100 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
         h->rows_dev = h->blk;
         h->pitchTb = (int64_t)round_up((size_t)(h->blk + 3) / 4, 128);
         for (int b = 0; b < 2; ++b) {
-            DPCA_TRY(dalloc(&h->Pb[b], (size_t)h->blk * h->pitch));
+            DPCA_TRY(dalloc(h, &h->Pb[b], (size_t)h->blk * h->pitch));
             DPCA_CUDA(cudaMemsetAsync(h->Pb[b], 0, (size_t)h->blk * h->pitch, h->stream));
             if (precision == DPCA_PREC_MIXED) {
-                DPCA_TRY(dalloc(&h->PTb[b], round_up((size_t)n_ind, 128) * h->pitchTb));
+                DPCA_TRY(dalloc(h, &h->PTb[b], round_up((size_t)n_ind, 128) * h->pitchTb));
                 DPCA_CUDA(cudaMemsetAsync(h->PTb[b], 0, round_up((size_t)n_ind, 128) * h->pitchTb, h->stream));
             }
             DPCA_CUDA(cudaEventCreateWithFlags(&h->copied[b], cudaEventDisableTiming));
             DPCA_CUDA(cudaEventCreateWithFlags(&h->consumed[b], cudaEventDisableTiming));
+            // the first copy into buffer b (copy stream) waits for its zeroing (compute stream)
+            DPCA_CUDA(cudaEventRecord(h->consumed[b], h->stream));
         }
         DPCA_CUDA(cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking));
     } else {
-        DPCA_TRY(dalloc(&h->P, (size_t)n_snp * h->pitch));
+        DPCA_TRY(dalloc(h, &h->P, (size_t)n_snp * h->pitch));
         DPCA_CUDA(cudaMemsetAsync(h->P, 0, (size_t)n_snp * h->pitch, h->stream));
     }
-    DPCA_TRY(dalloc(&h->counts, 4 * (size_t)n_snp));
-    DPCA_TRY(dalloc(&h->avg, (size_t)n_snp));
-    DPCA_TRY(dalloc(&h->sd, (size_t)n_snp));
-    DPCA_TRY(dalloc(&h->lut, 4 * (size_t)n_snp));
-    DPCA_TRY(dalloc(&h->coef, 2 * (size_t)n_snp));
-    DPCA_TRY(dalloc(&h->omega, nk));
-    DPCA_TRY(dalloc(&h->z, nk));
-    DPCA_TRY(dalloc(&h->q, nk));
-    DPCA_TRY(dalloc(&h->old, nk));
-    DPCA_TRY(dalloc(&h->work, nk));
-    DPCA_TRY(dalloc(&h->y, (size_t)h->rows_dev * nrhs));
+    DPCA_TRY(dalloc(h, &h->counts, 4 * (size_t)n_snp));
+    DPCA_TRY(dalloc(h, &h->avg, (size_t)n_snp));
+    DPCA_TRY(dalloc(h, &h->sd, (size_t)n_snp));
+    DPCA_TRY(dalloc(h, &h->lut, 4 * (size_t)n_snp));
+    DPCA_TRY(dalloc(h, &h->coef, 2 * (size_t)n_snp));
+    DPCA_TRY(dalloc(h, &h->omega, nk));
+    DPCA_TRY(dalloc(h, &h->z, nk));
+    DPCA_TRY(dalloc(h, &h->q, nk));
+    DPCA_TRY(dalloc(h, &h->old, nk));
+    DPCA_TRY(dalloc(h, &h->work, nk));
+    DPCA_TRY(dalloc(h, &h->y, (size_t)h->rows_dev * nrhs));
     // FP64 split-K partials: up to ceil(4*SMs / tiles) splits
     {
         int tiles = (n_ind + 127) / 128;
         int s = std::max(1, (4 * h->sm_count + tiles - 1) / tiles);
         s = std::min(s, std::max(1, (h->rows_dev + 31) / 32));
         h->partial_elems = (size_t)s * nk;
-        DPCA_TRY(dalloc(&h->partial, h->partial_elems));
+        DPCA_TRY(dalloc(h, &h->partial, h->partial_elems));
     }
     SmallLayout L{nrhs};
-    DPCA_TRY(dalloc(&h->small, L.total()));
+    DPCA_TRY(dalloc(h, &h->small, L.total()));
     DPCA_CUDA(cudaMemsetAsync(h->small, 0, L.total() * sizeof(double), h->stream));
     h->red_elems = std::max<size_t>({(size_t)2 * h->sm_count * (size_t)nrhs * nrhs,
                                      (size_t)4 * h->sm_count * (nrhs + 1), (size_t)nrhs * nrhs + 64});
-    DPCA_TRY(dalloc(&h->red, h->red_elems));
-    DPCA_TRY(dalloc(&h->dflag, 16));
+    DPCA_TRY(dalloc(h, &h->red, h->red_elems));
+    DPCA_TRY(dalloc(h, &h->dflag, 16));
     DPCA_CUDA(cudaMemsetAsync(h->dflag, 0, 16 * sizeof(int), h->stream));
-    DPCA_CUDA(cudaMallocHost((void **)&h->host_small, L.total() * sizeof(double)));
+    if (h->async_alloc) {
+        // pageable: pinned allocation and release can synchronise the device
+        h->host_small = (double *)calloc(L.total(), sizeof(double));
+        if (!h->host_small) return DPCA_ERR_NOMEM;
+    } else {
+        DPCA_CUDA(cudaMallocHost((void **)&h->host_small, L.total() * sizeof(double)));
+    }
     if (precision == DPCA_PREC_MIXED) {
         if (!h->streamed) {
             // tile-blocked (see transpose_packed_kernel): rows padded to whole 128-row tiles
-            DPCA_TRY(dalloc(&h->PT, round_up((size_t)n_ind, 128) * h->pitchT));
+            DPCA_TRY(dalloc(h, &h->PT, round_up((size_t)n_ind, 128) * h->pitchT));
             DPCA_CUDA(cudaMemsetAsync(h->PT, 0, round_up((size_t)n_ind, 128) * h->pitchT, h->stream));
         }
         DPCA_TRY(mixed_prepare(h));
     }
     h->clock.enabled = env_flag("DPCA_KERNEL_CLOCK");
+    return DPCA_OK;
+}
+
+size_t handle_footprint(int n_ind, int n_snp, int nrhs, int precision, int sm_count) {
+    const size_t np = (size_t)(n_ind + 3) / 4, pitch = round_up(np, 128);
+    const size_t nk = (size_t)n_ind * nrhs;
+    const int tiles = (n_ind + 127) / 128;
+    int s = std::max(1, (4 * sm_count + tiles - 1) / tiles);
+    s = std::min(s, std::max(1, (n_snp + 31) / 32));
+    const size_t L = SmallLayout{nrhs}.total();
+    const size_t red = std::max<size_t>({(size_t)2 * sm_count * (size_t)nrhs * nrhs,
+                                         (size_t)4 * sm_count * (nrhs + 1), (size_t)nrhs * nrhs + 64});
+    size_t b = (size_t)n_snp * pitch + (size_t)n_snp * (16 + 8 + 8 + 32 + 16) + 5 * nk * 8 +
+               (size_t)n_snp * nrhs * 8 + (size_t)s * nk * 8 + L * 8 + red * 8 + 64;
+    if (precision == DPCA_PREC_MIXED)
+        b += round_up((size_t)n_ind, 128) * round_up((size_t)(n_snp + 3) / 4, 128) +
+             mixed_footprint(n_ind, n_snp, nrhs, sm_count);
+    return b;
+}
+
+dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device,
+                                  cudaStream_t stream, int coop_blocks) {
+    *out = nullptr;
+    dpca_handle *hh = new (std::nothrow) dpca_handle();
+    if (!hh) return DPCA_ERR_NOMEM;
+    hh->h.async_alloc = true;
+    hh->h.coop_blocks = std::max(1, coop_blocks);
+    hh->h.stream = stream;  // set before create_impl so that its allocations are ordered on it
+    dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream, 0);
+    if (st != DPCA_OK) {
+        free_all(&hh->h);
+        delete hh;
+        return st;
+    }
+    *out = hh;
     return DPCA_OK;
 }
 
@@ -472,10 +552,14 @@ static dpca_status upload_pipelined(Handle *h, const uint8_t *packed, int64_t ro
         if (!h->copied[b]) check(cudaEventCreateWithFlags(&h->copied[b], cudaEventDisableTiming), "event");
         if (!h->consumed[b]) check(cudaEventCreateWithFlags(&h->consumed[b], cudaEventDisableTiming), "event");
         if (!direct && (!h->Sb[b] || h->sb_bytes < (size_t)rows_per * row_stride)) {
-            if (h->Sb[b]) cudaFree(h->Sb[b]);
+            dev_free(h, h->Sb[b]);
             h->Sb[b] = nullptr;
-            check(cudaMalloc(&h->Sb[b], (size_t)rows_per * row_stride), "staging");
+            if (st == DPCA_OK) st = dev_alloc(h, (void **)&h->Sb[b], (size_t)rows_per * row_stride);
         }
+        // the copy stream's first use of each buffer waits for everything queued on the compute
+        // stream so far: the allocations (stream-ordered ones are usable from that point) and
+        // the zeroing of P
+        check(cudaEventRecord(h->consumed[b], h->stream), "record");
     }
     if (!direct && st == DPCA_OK) h->sb_bytes = (size_t)rows_per * row_stride;
     cudaStream_t cs = h->cstream;
@@ -574,10 +658,11 @@ dpca_status dpca_upload(dpca_handle *hh, const uint8_t *packed, int64_t row_stri
         h->host_stride = row_stride;
         if (row_stride != h->pitch) {
             for (int b = 0; b < 2; ++b) {
-                if (h->Sb[b]) cudaFree(h->Sb[b]);
+                dev_free(h, h->Sb[b]);  // the compute stream is ordered after every copy that used it
                 h->Sb[b] = nullptr;
-                DPCA_TRY(dalloc(&h->Sb[b], (size_t)h->blk * row_stride));
+                DPCA_TRY(dalloc(h, &h->Sb[b], (size_t)h->blk * row_stride));
                 h->sb_bytes = (size_t)h->blk * row_stride;
+                DPCA_CUDA(cudaEventRecord(h->consumed[b], h->stream));
             }
         }
         DPCA_TRY(after_data(h));
@@ -601,17 +686,25 @@ dpca_status dpca_synth_fill(dpca_handle *hh, uint64_t key, const uint8_t *pop, c
     DPCA_CUDA(cudaSetDevice(h->device));
     uint8_t *d_pop = nullptr;
     uint32_t *d_miss = nullptr, *d_thr = nullptr;
-    DPCA_TRY(dalloc(&d_pop, (size_t)h->n_ind));
-    DPCA_TRY(dalloc(&d_miss, (size_t)h->n_ind));
-    DPCA_TRY(dalloc(&d_thr, (size_t)h->n_snp * n_pop));
+    const size_t held = h->dev_bytes;
+    dpca_status st = dalloc(h, &d_pop, (size_t)h->n_ind);
+    if (st == DPCA_OK) st = dalloc(h, &d_miss, (size_t)h->n_ind);
+    if (st == DPCA_OK) st = dalloc(h, &d_thr, (size_t)h->n_snp * n_pop);
+    if (st != DPCA_OK) {
+        dev_free(h, d_pop);
+        dev_free(h, d_miss);
+        h->dev_bytes = held;
+        return st;
+    }
     DPCA_CUDA(cudaMemcpyAsync(d_pop, pop, (size_t)h->n_ind, cudaMemcpyHostToDevice, h->stream));
     DPCA_CUDA(cudaMemcpyAsync(d_miss, miss_thr, (size_t)h->n_ind * 4, cudaMemcpyHostToDevice, h->stream));
     DPCA_CUDA(cudaMemcpyAsync(d_thr, snp_thr, (size_t)h->n_snp * n_pop * 4, cudaMemcpyHostToDevice, h->stream));
-    dpca_status st = launch_synth_fill(h, key, d_pop, d_miss, d_thr, n_pop);
-    cudaStreamSynchronize(h->stream);
-    cudaFree(d_pop);
-    cudaFree(d_miss);
-    cudaFree(d_thr);
+    st = launch_synth_fill(h, key, d_pop, d_miss, d_thr, n_pop);
+    cudaStreamSynchronize(h->stream);  // the host tables may be freed once this returns
+    dev_free(h, d_pop);
+    dev_free(h, d_miss);
+    dev_free(h, d_thr);
+    h->dev_bytes = held;  // temporaries
     DPCA_TRY(st);
     DPCA_TRY(after_data(h));
     return DPCA_OK;

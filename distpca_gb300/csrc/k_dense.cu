@@ -142,11 +142,19 @@ __global__ void __launch_bounds__(kQrThreads) hh_qr_kernel(double *__restrict__ 
 dpca_status launch_qr(Handle *h, double *a) {
     ScopedLaunch t(&h->clock, h->stream, "hh_qr");
     int n = h->n_ind, k = h->k;
-    static int max_blocks_per_sm = -1;
-    if (max_blocks_per_sm < 0)
-        DPCA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks_per_sm, hh_qr_kernel, kQrThreads, 0));
-    // one block per SM at most: every block sums all G partials after each barrier
+    // one block per SM at most (every block sums all G partials after each barrier), and only
+    // if the kernel fits an SM at all; the query runs once, thread-safely (handles of the
+    // serving loop launch from several host threads)
+    static const int max_blocks_per_sm = [] {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, hh_qr_kernel, kQrThreads, 0) != cudaSuccess) {
+            cudaGetLastError();
+            v = 1;
+        }
+        return v;
+    }();
     int maxg = std::min(std::max(1, max_blocks_per_sm), 1) * h->sm_count;
+    if (h->coop_blocks > 0) maxg = std::min(maxg, h->coop_blocks);
     int G = std::max(1, std::min(maxg, ceil_div(n, 64)));
     int rpb = ceil_div(n, G);
     G = ceil_div(n, rpb);
@@ -219,7 +227,7 @@ dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, doubl
     size_t smem = (size_t)2 * 32 * k * sizeof(double);
     {
         ScopedLaunch t(&h->clock, h->stream, "atb");
-        cudaFuncSetAttribute(atb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_smem((const void *)atb_kernel);
         atb_kernel<<<nparts, 256, smem, h->stream>>>(a, b, n, k, rpb, h->red);
         DPCA_CUDA(cudaGetLastError());
     }
@@ -331,7 +339,7 @@ dpca_status launch_eig_desc(Handle *h) {
     int k = h->k;
     SmallLayout L{k};
     size_t smem = (size_t)k * (k + 1) * sizeof(double) + 2 * 64 * sizeof(double) + (k + 2) * sizeof(int);
-    DPCA_CUDA(cudaFuncSetAttribute(jacobi_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DPCA_TRY(allow_max_smem((const void *)jacobi_eig_kernel));
     jacobi_eig_kernel<<<1, 512, smem, h->stream>>>(h->small + L.B(), k, h->small + L.W(), h->small + L.w(), h->red,
                                                    60);
     DPCA_CUDA(cudaGetLastError());
@@ -359,7 +367,7 @@ dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
     ScopedLaunch t(&h->clock, h->stream, "apply_w");
     int k = h->k;
     size_t smem = (size_t)k * k * sizeof(double);
-    DPCA_CUDA(cudaFuncSetAttribute(apply_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DPCA_TRY(allow_max_smem((const void *)apply_w_kernel));
     int64_t total = (int64_t)h->n_ind * k;
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
     apply_w_kernel<<<grid, 256, smem, h->stream>>>(q, h->small + SmallLayout{k}.W(), h->n_ind, k, out);

@@ -142,7 +142,7 @@ template <int MAXC>
 static void xw_launch(Handle *h, const double *omega, double *y) {
     size_t smem = (size_t)64 * h->k * sizeof(double);
     // opt in above the default 48 KB (static shared memory counts against it as well)
-    cudaFuncSetAttribute(fp64_xw_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_smem((const void *)fp64_xw_kernel<MAXC>);
     fp64_xw_kernel<MAXC><<<ceil_div(h->n_snp, 64), 256, smem, h->stream>>>(h->P, h->pitch, h->lut, h->n_ind,
                                                                             h->n_snp, h->k, omega, y);
 }
@@ -171,7 +171,7 @@ static int xty_splits(const Handle *h) {
 template <int MAXC>
 static void xty_launch(Handle *h, const double *y, int splits, int sps) {
     size_t smem = (size_t)32 * h->k * sizeof(double);
-    cudaFuncSetAttribute(fp64_xty_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_smem((const void *)fp64_xty_kernel<MAXC>);
     dim3 grid(ceil_div(h->n_ind, 128), splits);
     fp64_xty_kernel<MAXC><<<grid, 512, smem, h->stream>>>(h->P, h->pitch, h->lut, h->n_ind, h->n_snp, h->k, y,
                                                            h->partial, sps);
@@ -257,7 +257,7 @@ template <int MAXC>
 static void xw_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
                           const double *omega, double *y, cudaStream_t st) {
     size_t smem = (size_t)64 * k * sizeof(double);
-    cudaFuncSetAttribute(fp64_xw_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_smem((const void *)fp64_xw_kernel<MAXC>);
     fp64_xw_kernel<MAXC><<<ceil_div(n_snp, 64), 256, smem, st>>>(P, pitch, lut, n_ind, n_snp, k, omega, y);
 }
 
@@ -265,7 +265,7 @@ template <int MAXC>
 static void xty_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
                            const double *y, double *partial, int splits, int sps, cudaStream_t st) {
     size_t smem = (size_t)32 * k * sizeof(double);
-    cudaFuncSetAttribute(fp64_xty_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_smem((const void *)fp64_xty_kernel<MAXC>);
     dim3 grid(ceil_div(n_ind, 128), splits);
     fp64_xty_kernel<MAXC><<<grid, 512, smem, st>>>(P, pitch, lut, n_ind, n_snp, k, y, partial, sps);
 }

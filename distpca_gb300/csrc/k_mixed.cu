@@ -659,27 +659,20 @@ dpca_status mixed_prepare(Handle *h) {
     }
     // SNP-indexed operands cover the rows resident at a time (all SNPs, or one streamed block)
     const int rows_pad = (h->rows_dev + 127) / 128 * 128;
-    cudaError_t e;
     size_t om_elems = (size_t)N * h->n_ind_pad, bop_elems = (size_t)2 * N * rows_pad;
-    if ((e = cudaMalloc(&m->omega_s, om_elems * 2)) != cudaSuccess ||
-        (e = cudaMalloc(&m->bop, bop_elems * 2)) != cudaSuccess ||
-        (e = cudaMalloc(&m->scales, 4 * (size_t)k * 8)) != cudaSuccess ||
-        (e = cudaMalloc(&m->yt, (size_t)k * rows_pad * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&m->colmax, (size_t)k * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&m->colsumq, (size_t)k * 8)) != cudaSuccess ||
-        (e = cudaMalloc(&m->rq, (size_t)k * 8)) != cudaSuccess) {
-        set_error("mixed operand allocation: %s", cudaGetErrorString(e));
-        return DPCA_ERR_NOMEM;
-    }
+    DPCA_TRY(dev_alloc(h, (void **)&m->omega_s, om_elems * 2));
+    DPCA_TRY(dev_alloc(h, (void **)&m->bop, bop_elems * 2));
+    DPCA_TRY(dev_alloc(h, (void **)&m->scales, 4 * (size_t)k * 8));
+    DPCA_TRY(dev_alloc(h, (void **)&m->yt, (size_t)k * rows_pad * 4));
+    DPCA_TRY(dev_alloc(h, (void **)&m->colmax, (size_t)k * 4));
+    DPCA_TRY(dev_alloc(h, (void **)&m->colsumq, (size_t)k * 8));
+    DPCA_TRY(dev_alloc(h, (void **)&m->rq, (size_t)k * 8));
     DPCA_CUDA(cudaMemsetAsync(m->omega_s, 0, om_elems * 2, h->stream));
     DPCA_CUDA(cudaMemsetAsync(m->bop, 0, bop_elems * 2, h->stream));
     pick_splits(h, h->rows_dev, &m->kb_per_split, &m->splits);
     // a shorter (last) streamed block may pick more splits: room for the most the rule allows
     m->splits_cap = h->streamed ? 16 : m->splits;
-    if ((e = cudaMalloc(&m->partial, (size_t)m->splits_cap * h->n_ind * k * 8)) != cudaSuccess) {
-        set_error("mixed partial allocation: %s", cudaGetErrorString(e));
-        return DPCA_ERR_NOMEM;
-    }
+    DPCA_TRY(dev_alloc(h, (void **)&m->partial, (size_t)m->splits_cap * h->n_ind * k * 8));
     m->ring1 = pick_ring(kXW, N, m->kp);
     m->ring2 = pick_ring(kXTY, N, m->kp);
     m->smem1 = smem_bytes(kXW, N, m->kp, m->ring1);
@@ -698,18 +691,29 @@ dpca_status mixed_prepare(Handle *h) {
     }
     DPCA_TRY(make_batch_map(&m->map_om, m->omega_s, h->n_ind_pad, N));
     DPCA_TRY(make_batch_map(&m->map_bop, m->bop, rows_pad, 2 * N));
-    DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem1));
-    DPCA_CUDA(cudaFuncSetAttribute(mixed_gemm_kernel<kXTY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)m->smem2));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW>));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY>));
     return DPCA_OK;
+}
+
+// Device bytes mixed_prepare allocates for a resident handle.
+size_t mixed_footprint(int n_ind, int n_snp, int nrhs, int sm_count) {
+    Handle t;
+    t.n_ind = n_ind;
+    t.sm_count = sm_count;
+    int kbps = 8, splits = 1;
+    pick_splits(&t, n_snp, &kbps, &splits);
+    const size_t kp = (size_t)(nrhs + 7) / 8 * 8, N = 2 * kp;
+    const size_t n_pad = (size_t)(n_ind + 127) / 128 * 128, rows_pad = (size_t)(n_snp + 127) / 128 * 128;
+    return N * n_pad * 2 + 2 * N * rows_pad * 2 + 4 * (size_t)nrhs * 8 + (size_t)nrhs * rows_pad * 4 +
+           (size_t)nrhs * 20 + (size_t)splits * n_ind * nrhs * 8;
 }
 
 dpca_status mixed_release(Handle *h) {
     MixedState *m = mstate(h);
     if (!m) return DPCA_OK;
     void *ptrs[] = {m->omega_s, m->bop, m->yt, m->colmax, m->scales, m->partial, m->colsumq, m->rq};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    for (void *p : ptrs) dev_free(h, p);
     delete m;
     h->mx = nullptr;
     return DPCA_OK;

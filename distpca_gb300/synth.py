@@ -200,3 +200,30 @@ def config_cohort(name: str, n_snp: Optional[int] = None, n_ind: Optional[int] =
         return make_cohort(n_ind or 500_000, n_snp or 2_000_000, n_pop=10, fst=0.01, p_beta=(0.5, 2.0),
                            p_clip=(0.005, 0.5), missing=0.0, heavy_frac=0.1, heavy_rate=0.5, seed=3)
     raise KeyError(name)
+
+
+def serve_stream(n_jobs: int = 512, rate: float = 50.0, seed: int = 0) -> list:
+    """A mixed-size PCA job stream: Poisson arrivals at `rate` jobs/s.
+
+    Per job, seeded independently: n_ind log-uniform in [500, 20,000], n_snp log-uniform in
+    [10,000, 500,000], nsv uniform in {5, 10, 20}, nrhs = 2 nsv, power 4, a Balding-Nichols
+    cohort with K uniform in 2..8 populations, Fst uniform in [0.01, 0.1] and 0-3% missing.
+    Returns dicts with the arrival time `t` (s), the sizes, the run flags and the cohort
+    parameters (make_cohort draws the tables)."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_jobs))
+    jobs = []
+    for j in range(n_jobs):
+        n = int(round(float(np.exp(rng.uniform(np.log(500), np.log(20000))))))
+        m = int(round(float(np.exp(rng.uniform(np.log(1e4), np.log(5e5))))))
+        nsv = int(rng.choice([5, 10, 20]))
+        jobs.append(dict(t=float(arrivals[j]), n_ind=n, n_snp=m, nsv=nsv, nrhs=2 * nsv, power=4,
+                         n_pop=int(rng.integers(2, 9)), fst=float(rng.uniform(0.01, 0.1)),
+                         missing=float(rng.uniform(0.0, 0.03)), seed=seed * 1000003 + j + 1))
+    return jobs
+
+
+def serve_cohort(job: dict) -> Cohort:
+    """The cohort tables of one serve_stream job."""
+    return make_cohort(job["n_ind"], job["n_snp"], n_pop=job["n_pop"], fst=job["fst"], missing=job["missing"],
+                       seed=job["seed"])

@@ -213,6 +213,67 @@ dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_
 dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp,
                                    const double *omega, int nrhs, double *z, void *stream);
 
+/* ---- serving loop: many independent PCA jobs on one GPU ----
+ * The reference runs one PCA per MPI job: main reads one .bed and calls the solver once
+ * (src/distpca.cpp:83-405 -> BlockSubspaceIter_MPI_OOC_double_buffering, src/methods.h:49).
+ * A dpca_server accepts such jobs as they arrive -- different cohorts, SNP sets, nsv and nrhs --
+ * and runs up to `slots` of them at once on one device, each on its own stream and host worker
+ * thread.  Admission: in arrival order, when a slot is free and the job's device footprint fits
+ * the memory budget beside the jobs in flight; a later job that fits may pass one that does not
+ * fit yet, at most 2*slots times for that job.  A job's packed genotypes and subspace state stay
+ * on the device until it finishes.  Its buffers are stream-ordered allocations from the device's
+ * memory pool, so admitting and retiring jobs never synchronises the device under the other
+ * jobs' work.  A job's result is the one dpca_solve gives for the same inputs alone: the kernels
+ * are deterministic and jobs share no device state.  Jobs larger than the whole budget fail with
+ * DPCA_ERR_NOMEM at submission. */
+typedef struct dpca_server dpca_server;
+
+typedef struct {
+    int device;
+    int slots;            /* jobs in flight at once, 1..64 (0: 4) */
+    double hbm_budget_gb; /* device memory the jobs in flight may hold (<= 0: 85% of the free memory) */
+} dpca_serve_config;
+
+typedef struct {
+    int n_ind, n_snp;
+    /* nsv, nrhs, power, crit, tol, miter, precision; bsize >= n_snp selects the in-core variant.
+     * verbose, fwrite, full_svd, prefix, memory_gb, device and hbm_budget_gb are not used. */
+    dpca_config cfg;
+    /* Genotypes: packed host rows (SNP-major, .bed bytes, row_stride >= ceil(n_ind/4) apart), or,
+     * when packed is NULL, a seeded Balding-Nichols cohort filled on the device from the
+     * dpca_synth_fill tables.  Every array must stay valid until the job is done. */
+    const uint8_t *packed;
+    int64_t row_stride;
+    uint64_t synth_key;
+    const uint8_t *synth_pop;        /* [n_ind] */
+    const uint32_t *synth_miss_thr;  /* [n_ind] */
+    const uint32_t *synth_snp_thr;   /* [n_snp * synth_n_pop] */
+    int synth_n_pop;
+    const double *omega;  /* start block n_ind x nrhs, or NULL for dpca_start_block's */
+    double *sigma;        /* [nsv], written when the job is done */
+    double *u;            /* [n_ind * nsv] or NULL, written when the job is done */
+} dpca_job;
+
+typedef struct {
+    int status;           /* dpca_status of the job */
+    int total_its, passes;
+    double t_submit, t_start, t_done;  /* seconds since dpca_serve_create */
+    double device_gb;     /* footprint admitted against the budget */
+    char error[256];
+} dpca_job_info;
+
+dpca_status dpca_serve_create(dpca_server **out, const dpca_serve_config *cfg);
+/* Queue a job; thread-safe.  The dpca_job is copied, the arrays it points to are not. */
+dpca_status dpca_serve_submit(dpca_server *s, const dpca_job *job, int64_t *job_id);
+/* Non-blocking: *done = 1 and *info (may be NULL) filled once the job has finished. */
+dpca_status dpca_serve_poll(dpca_server *s, int64_t job_id, int *done, dpca_job_info *info);
+/* Block until the job has finished (DPCA_ERR_TIMEOUT after timeout_s seconds; < 0 waits forever). */
+dpca_status dpca_serve_wait(dpca_server *s, int64_t job_id, double timeout_s, dpca_job_info *info);
+/* Jobs finished, most jobs in flight at once, most device bytes admitted at once, the budget. */
+dpca_status dpca_serve_stats(dpca_server *s, int64_t *done, int *max_in_flight, double *peak_gb, double *budget_gb);
+/* Finish every submitted job, stop the workers and free the server. */
+dpca_status dpca_serve_shutdown(dpca_server *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -179,3 +179,32 @@ def test_full_svd_limits_checked_before_the_device(dpca):
     with pytest.raises(dpca.DpcaError) as e:
         dpca.full_svd(r, 30_000, 4, packed=packed, nsv=3, nrhs=6)
     assert e.value.status == 6
+
+
+def test_serving_struct_layouts_match_the_header(dpca, tmp_path):
+    """The ctypes mirrors of dpca_serve_config, dpca_job and dpca_job_info have the C layout."""
+    import shutil
+    import subprocess
+
+    from distpca_gb300 import api
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"dpca_serve_config": api.ServeConfig, "dpca_job": api.Job, "dpca_job_info": api.JobInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "dpca.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call([cc, "-I", os.path.join(root, "include"), str(src), "-o", str(exe)])
+    got = dict(line.rsplit(" ", 1) for line in subprocess.check_output([str(exe)]).decode().splitlines())
+    for cname, py in structs.items():
+        assert int(got[f"{cname} size"]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[f"{cname} {f}"]) == getattr(py, f).offset, (cname, f)
