@@ -51,6 +51,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the accuracy solve")
+    p.add_argument("--no-serve", action="store_true", help="skip the serving-loop job stream")
+    p.add_argument("--serve-jobs", type=int, default=512)
+    p.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (jobs/s)")
+    p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--serve-sample", type=int, default=8, help="jobs in the one-at-a-time FP64 comparison")
     return p.parse_args()
 
 
@@ -314,6 +319,8 @@ def dpca_arm(a, ranks: Ranks) -> None:
         line["e2e"] = e2e_run(a, hv)
     if ranks.rank == 0 and not a.no_extras:
         line["streamed"] = streamed_run(a, hv)
+    if ranks.rank == 0 and not a.no_serve:
+        line["serve"] = serve_run(a)
     if ranks.rank == 0 and not a.no_cpu and ranks.world == 1:
         line["cpu_baseline"] = cpu_baseline(a, hv)
     if ranks.rank == 0:
@@ -419,6 +426,59 @@ def streamed_run(a, hv) -> dict:
     return {"value": a.n_ind * a.n_snp / t, "unit": UNIT, "ms_per_pass": t * 1e3,
             "h2d_gbs": hv.nbytes / t / 1e9, "block_snps": blk, "blocks": (a.n_snp + blk - 1) // blk,
             "note": "rows in pinned host memory, two device blocks double-buffered on a copy stream"}
+
+
+def serve_run(a) -> dict:
+    """The mixed-size job stream through the serving loop (dpca_serve_*): Poisson arrivals of
+    seeded Balding-Nichols jobs (n_ind log-U[500, 20k], n_snp log-U[10k, 500k], nsv in {5, 10, 20},
+    nrhs 2 nsv, power 4; the reference's defaults crit 1, tol 1e-3), each job's genotypes filled
+    on the device.  Latency = completion - submission.  Beside it, jobs of the same stream run one
+    at a time as plain FP64 GPU solves and as mixed solves (the first jobs of at most 2e8
+    genotypes, which bounds the FP64 arm's time)."""
+    import distpca_gb300 as D
+    from distpca_gb300 import synth
+
+    jobs = synth.serve_stream(a.serve_jobs, a.serve_rate, seed=0)
+    cohorts = [synth.serve_cohort(j) for j in jobs]
+
+    def flags(j, prec):
+        return dict(nsv=j["nsv"], nrhs=j["nrhs"], power=j["power"], bsize=j["n_snp"], precision=prec)
+
+    with D.Server(slots=a.serve_slots) as s:
+        ids = []
+        start = time.perf_counter()
+        for j, c in zip(jobs, cohorts):
+            d = start + j["t"] - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            ids.append(s.submit(j["n_ind"], j["n_snp"], cohort=c, want_u=False, **flags(j, "mixed")))
+        res = [s.result(i) for i in ids]
+        wall = time.perf_counter() - start
+        st = s.stats()
+    lat = np.array([r["info"].t_done - r["info"].t_submit for r in res])
+    svc = np.array([r["info"].t_done - r["info"].t_start for r in res])
+    gpass = sum(j["n_ind"] * j["n_snp"] * r["passes"] for j, r in zip(jobs, res))
+    picked = [i for i, j in enumerate(jobs) if j["n_ind"] * j["n_snp"] <= 2e8][:a.serve_sample]
+
+    def one_at_a_time(prec):
+        with D.Server(slots=1) as s:
+            out = []
+            for i in picked:
+                j = jobs[i]
+                r = s.result(s.submit(j["n_ind"], j["n_snp"], cohort=cohorts[i], want_u=False, **flags(j, prec)))
+                out.append(r["info"].t_done - r["info"].t_start)
+        return float(sum(out))
+
+    t64, tmx = one_at_a_time("fp64"), one_at_a_time("mixed")
+    return {"jobs": len(jobs), "arrival_rate_per_s": a.serve_rate, "slots": a.serve_slots,
+            "wall_s": wall, "jobs_per_s": len(jobs) / wall, "latency_p50_s": float(np.median(lat)),
+            "latency_p99_s": float(np.quantile(lat, 0.99)), "service_p50_s": float(np.median(svc)),
+            "genotype_passes_per_s": gpass / wall, "max_in_flight": st["max_in_flight"],
+            "peak_device_gb": st["peak_gb"], "budget_gb": st["budget_gb"],
+            "one_at_a_time": {"sample": f"jobs {picked} of the stream (the first {len(picked)} of <= 2e8 genotypes)",
+                              "fp64_gpu_s": t64, "mixed_s": tmx, "fp64_jobs_per_s": len(picked) / t64,
+                              "mixed_jobs_per_s": len(picked) / tmx},
+            "data": "seeded Balding-Nichols cohorts filled on the device per job"}
 
 
 def cpu_baseline(a, hv) -> dict:

@@ -17,7 +17,7 @@ import numpy as np
 
 __all__ = ["DpcaError", "Config", "Result", "Handle", "lib", "library_path", "config", "parse_args", "probe",
            "resolve", "start_block", "run", "run_packed", "decode_counts", "PREC_FP64", "PREC_MIXED",
-           "exported_symbols", "FullSVD", "full_svd", "Server", "JobInfo"]
+           "exported_symbols", "FullSVD", "full_svd", "Server", "JobInfo", "sym_eig"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PREC_FP64 = 0
@@ -91,6 +91,7 @@ _SIGS = {
     "dpca_resolve_config": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_int)]),
     "dpca_start_block": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "dpca_sym_eig": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "dpca_run": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(Result)]),
     "dpca_run_packed": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(Result)]),
@@ -209,6 +210,17 @@ def start_block(n_ind: int, k: int) -> np.ndarray:
     out = np.empty((n_ind, k), dtype=np.float64)
     _check(lib().dpca_start_block(n_ind, k, _p(out)))
     return out
+
+
+def sym_eig(b: np.ndarray):
+    """Eigenvalues (descending) and eigenvectors (columns) of the symmetric matrix b (upper triangle
+    used): the solve's Rayleigh-Ritz eigenproblem, computed on the host."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    k = b.shape[0]
+    w = np.empty(k)
+    W = np.empty((k, k))
+    _check(lib().dpca_sym_eig(k, _p(b), _p(w), _p(W)))
+    return w, W
 
 
 def _result_arrays(c: Config, n_ind: int):

@@ -179,6 +179,7 @@ dpca_status launch_fp64_xty(Handle *h, const double *y, double *z);
 dpca_status launch_qr(Handle *h, double *a);
 dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, double *out);  // k x k = A^T B
 dpca_status launch_eig_desc(Handle *h);                                                   // small.B -> W, w
+dpca_status host_sym_eig_desc(int k, const double *B, double *w, double *W);              // eig_host.cpp
 dpca_status launch_apply_w(Handle *h, const double *q, double *out);                      // out = Q W
 dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol, int ii, const double *old,
                                        const double *omega);

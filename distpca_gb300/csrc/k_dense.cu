@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kQrThreads) hh_qr_kernel(double *__restrict__ 
     }
 }
 
-dpca_status launch_qr(Handle *h, double *a) {
+dpca_status launch_qr_householder(Handle *h, double *a) {
     ScopedLaunch t(&h->clock, h->stream, "hh_qr");
     int n = h->n_ind, k = h->k;
     // one block per SM at most (every block sums all G partials after each barrier), and only
@@ -217,23 +217,34 @@ __global__ void sum_parts_kernel(const double *__restrict__ part, int nparts, in
     }
 }
 
-dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, double *out) {
+// A^T B over n rows in two launches (block partials, then their sum), timed under the given names.
+static dpca_status atb_timed(Handle *h, const double *a, const double *b, int n, double *out, const char *name,
+                             const char *sum_name) {
     int k = h->k;
     int kk = k * k;
-    int nparts = std::max(1, std::min(2 * h->sm_count, ceil_div(n, 256)));
+    // FP64 is a small fraction of this GPU's arithmetic: spread the n k^2 FMAs over as many SMs
+    // as there are 32-row tiles (up to two blocks per SM)
+    int nparts = std::max(1, std::min(2 * h->sm_count, ceil_div(n, 32)));
     nparts = (int)std::min<int64_t>(nparts, (int64_t)(h->red_elems / kk));
     int rpb = ceil_div(n, nparts);
     nparts = ceil_div(n, rpb);
     size_t smem = (size_t)2 * 32 * k * sizeof(double);
+    DPCA_TRY(allow_max_smem((const void *)atb_kernel));
     {
-        ScopedLaunch t(&h->clock, h->stream, "atb");
-        allow_max_smem((const void *)atb_kernel);
+        ScopedLaunch t(&h->clock, h->stream, name);
         atb_kernel<<<nparts, 256, smem, h->stream>>>(a, b, n, k, rpb, h->red);
         DPCA_CUDA(cudaGetLastError());
     }
-    sum_parts_kernel<<<ceil_div(kk, 256), 256, 0, h->stream>>>(h->red, nparts, kk, out);
-    DPCA_CUDA(cudaGetLastError());
+    {
+        ScopedLaunch t(&h->clock, h->stream, sum_name);
+        sum_parts_kernel<<<ceil_div(kk, 256), 256, 0, h->stream>>>(h->red, nparts, kk, out);
+        DPCA_CUDA(cudaGetLastError());
+    }
     return DPCA_OK;
+}
+
+dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, double *out) {
+    return atb_timed(h, a, b, n, out, "atb", "atb_sum");
 }
 
 // ------------------------------------------------------------------ Jacobi eigensolver
@@ -334,15 +345,19 @@ __global__ void __launch_bounds__(512) jacobi_eig_kernel(const double *__restric
     }
 }
 
+// The k x k eigenproblem goes to the host (eig_host.cpp): B down, W and w (adjacent in the small
+// block) back up.  The event pair brackets the copies and the host solve.
 dpca_status launch_eig_desc(Handle *h) {
-    ScopedLaunch t(&h->clock, h->stream, "jacobi_eig");
-    int k = h->k;
-    SmallLayout L{k};
-    size_t smem = (size_t)k * (k + 1) * sizeof(double) + 2 * 64 * sizeof(double) + (k + 2) * sizeof(int);
-    DPCA_TRY(allow_max_smem((const void *)jacobi_eig_kernel));
-    jacobi_eig_kernel<<<1, 512, smem, h->stream>>>(h->small + L.B(), k, h->small + L.W(), h->small + L.w(), h->red,
-                                                   60);
-    DPCA_CUDA(cudaGetLastError());
+    ScopedLaunch t(&h->clock, h->stream, "sym_eig");
+    const int k = h->k;
+    const SmallLayout L{k};
+    DPCA_CUDA(cudaMemcpyAsync(h->host_small + L.B(), h->small + L.B(), (size_t)k * k * sizeof(double),
+                              cudaMemcpyDeviceToHost, h->stream));
+    DPCA_CUDA(cudaStreamSynchronize(h->stream));
+    DPCA_TRY(check_device_flag(h));
+    DPCA_TRY(host_sym_eig_desc(k, h->host_small + L.B(), h->host_small + L.w(), h->host_small + L.W()));
+    DPCA_CUDA(cudaMemcpyAsync(h->small + L.W(), h->host_small + L.W(), ((size_t)k * k + k) * sizeof(double),
+                              cudaMemcpyHostToDevice, h->stream));
     return DPCA_OK;
 }
 
@@ -372,6 +387,113 @@ dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
     apply_w_kernel<<<grid, 256, smem, h->stream>>>(q, h->small + SmallLayout{k}.W(), h->n_ind, k, out);
     DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
+// ------------------------------------------------------------------ shifted CholeskyQR3
+// Thin QR of the n x k panel A (in place, Q only) by three CholeskyQR steps (Fukaya, Kannan,
+// Nakatsukasa, Yamamoto, Yanagisawa, "Shifted Cholesky QR for computing the QR factorization of
+// ill-conditioned matrices", SIAM J. Sci. Comput. 42 (2020)): G = A^T A, R = chol(G + s I),
+// A <- A R^-1, with the shift s = 11 (n k + k (k + 1)) u ||A||_F^2 in the first step, which keeps
+// the Cholesky factorization defined for condition numbers up to ~1/u (the reference's start
+// block has ~5e9), and then two plain steps (CholeskyQR2) that restore orthogonality to O(u).
+// The panel is read three times and written three times; no step needs a grid-wide barrier, so
+// the QR costs a dozen short launches instead of ~4k barriers of a column-by-column Householder
+// QR.  Q spans the same column space as the reference's dgeqrf + dorgqr (methods.cpp:947-961);
+// its columns may differ in sign, which the Rayleigh-Ritz step (methods.cpp:972-1007) absorbs:
+// the Ritz vectors come out with the eigensolver's signs either way.
+//
+// chol_inv_kernel (one block): G (k x k, from the Gram launch) -> R^-1 (upper triangular,
+// row-major k x k).  A non-positive or non-finite pivot in a plain step restarts that step with
+// the shift; a pivot that still fails (a panel with a zero or non-finite column) is replaced by 1,
+// which leaves that column unnormalised instead of dividing by zero.
+constexpr int kCholThreads = 256;
+
+__global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__restrict__ G, int k, int n,
+                                                                int always_shift, double *__restrict__ Rinv) {
+    extern __shared__ double g[];  // k x k, upper triangle -> R
+    __shared__ double sh_inv[kMaxNrhs];
+    __shared__ int broke;
+    const int tid = threadIdx.x;
+    double tr = 0.0;
+    for (int i = 0; i < k; ++i) tr += G[(size_t)i * k + i];  // every thread: same order, same value
+    const double shift = 11.0 * ((double)n * k + (double)k * (k + 1)) * 0x1p-53 * tr;
+    for (int attempt = always_shift ? 1 : 0; attempt < 2; ++attempt) {
+        for (int e = tid; e < k * k; e += kCholThreads) {
+            const int i = e / k, c = e - i * k;
+            g[e] = G[e] + (attempt == 1 && i == c ? shift : 0.0);
+        }
+        if (tid == 0) broke = 0;
+        __syncthreads();
+        const int tx = tid & 15, ty = tid >> 4;  // 16 x 16 map of the trailing block
+        for (int j = 0; j < k; ++j) {
+            // every thread reads the pivot and scales its share of row j by 1/sqrt(pivot)
+            double d = g[(size_t)j * k + j];
+            const bool bad = !(d > 0.0) || !isfinite(d);
+            if (bad) d = 1.0;
+            const double inv = rsqrt(d);
+            __syncthreads();  // everyone has read the pivot
+            if (tid == 0) {
+                if (bad) broke = 1;
+                g[(size_t)j * k + j] = d * inv;
+                sh_inv[j] = inv;
+            }
+            for (int c = j + 1 + tid; c < k; c += kCholThreads) g[(size_t)j * k + c] *= inv;
+            __syncthreads();
+            // trailing update of the upper triangle: g[a][b] -= r[j][a] r[j][b], j < a <= b
+            for (int a = j + 1 + ty; a < k; a += 16) {
+                const double rja = g[(size_t)j * k + a];
+                for (int b = a + tx; b < k; b += 16) g[(size_t)a * k + b] -= rja * g[(size_t)j * k + b];
+            }
+            __syncthreads();
+        }
+        if (!broke) break;
+        __syncthreads();
+    }
+    // R^-1 in place, column by column (the order of LAPACK's dtrti2): with the leading j x j block
+    // already inverted, column j above the diagonal is -(R^-1)_{0:j,0:j} R_{0:j,j} / R_jj; thread i
+    // computes row i (i < j <= k <= kMaxNrhs < kCholThreads)
+    for (int j = 0; j < k; ++j) {
+        double x = 0.0;
+        if (tid < j)
+            for (int l = tid; l < j; ++l) x = fma(g[(size_t)tid * k + l], g[(size_t)l * k + j], x);
+        __syncthreads();
+        if (tid < j) g[(size_t)tid * k + j] = -x * sh_inv[j];
+        if (tid == j) g[(size_t)j * k + j] = sh_inv[j];
+        __syncthreads();
+    }
+    for (int e = tid; e < k * k; e += kCholThreads) {
+        const int i = e / k, c = e - i * k;
+        Rinv[e] = c >= i ? g[e] : 0.0;
+    }
+}
+
+dpca_status launch_qr(Handle *h, double *a) {
+    const int n = h->n_ind, k = h->k;
+    const SmallLayout L{k};
+    double *G = h->small + L.B(), *Rinv = h->small + L.W();  // free until the Rayleigh-Ritz step
+    DPCA_TRY(allow_max_smem((const void *)chol_inv_kernel));
+    DPCA_TRY(allow_max_smem((const void *)apply_w_kernel));
+    const size_t smem_g = (size_t)k * k * sizeof(double);
+    const int64_t total = (int64_t)n * k;
+    const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
+    double *src = a, *dst = h->work;
+    for (int step = 0; step < 3; ++step) {
+        DPCA_TRY(atb_timed(h, src, src, n, G, "qr_gram", "qr_gram_sum"));
+        {
+            ScopedLaunch t(&h->clock, h->stream, "qr_chol");
+            chol_inv_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
+            DPCA_CUDA(cudaGetLastError());
+        }
+        {
+            ScopedLaunch t(&h->clock, h->stream, "qr_apply");
+            apply_w_kernel<<<grid, 256, smem_g, h->stream>>>(src, Rinv, n, k, dst);
+            DPCA_CUDA(cudaGetLastError());
+        }
+        std::swap(src, dst);
+    }
+    // three steps: a -> work -> a -> work
+    DPCA_CUDA(cudaMemcpyAsync(a, src, (size_t)total * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     return DPCA_OK;
 }
 

@@ -208,3 +208,29 @@ def test_serving_struct_layouts_match_the_header(dpca, tmp_path):
         assert int(got[f"{cname} size"]) == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert int(got[f"{cname} {f}"]) == getattr(py, f).offset, (cname, f)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 8, 20, 40, 97, 128])
+def test_sym_eig_matches_numpy(dpca, k):
+    """The host Rayleigh-Ritz eigensolver against numpy.linalg.eigh (LAPACK): eigenvalues within
+    1e-12 of the largest, eigenvectors orthonormal and A W = W diag(w) to 1e-12 relative."""
+    rng = np.random.default_rng(k)
+    cases = []
+    g = rng.standard_normal((k, k))
+    cases.append(g + g.T)                                   # indefinite
+    x = rng.standard_normal((3 * k + 5, k))
+    cases.append(x.T @ x)                                   # PSD, like Q^T Z
+    q, _ = np.linalg.qr(rng.standard_normal((k, k)))
+    lam = np.repeat(rng.standard_normal(k // 3 + 1), 3)[:k]
+    cases.append((q * lam) @ q.T)                           # clustered / repeated eigenvalues
+    cases.append(np.diag(rng.standard_normal(k)))           # already diagonal
+    cases.append(np.zeros((k, k)))
+    for a in cases:
+        upper = np.triu(a) + np.tril(rng.standard_normal((k, k)), -1) * 1e3  # the lower triangle is ignored
+        w, W = dpca.sym_eig(upper)
+        ref = np.linalg.eigvalsh(a)[::-1]
+        scale = max(1.0, np.abs(ref).max())
+        assert np.all(np.diff(w) <= 0)
+        np.testing.assert_allclose(w, ref, atol=1e-12 * scale, rtol=0)
+        np.testing.assert_allclose(W.T @ W, np.eye(k), atol=1e-12)
+        assert np.abs(a @ W - W * w).max() <= 1e-12 * scale
