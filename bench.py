@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the accuracy solve")
     p.add_argument("--no-serve", action="store_true", help="skip the serving-loop job stream")
+    p.add_argument("--no-windows", action="store_true", help="skip the batched-window local PCA")
+    p.add_argument("--windows", type=int, default=4096, help="SNP windows in the batched local PCA")
     p.add_argument("--serve-jobs", type=int, default=512)
     p.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (jobs/s)")
     p.add_argument("--serve-slots", type=int, default=8)
@@ -319,6 +321,8 @@ def dpca_arm(a, ranks: Ranks) -> None:
         line["e2e"] = e2e_run(a, hv)
     if ranks.rank == 0 and not a.no_extras:
         line["streamed"] = streamed_run(a, hv)
+    if ranks.rank == 0 and not a.no_windows:
+        line["windows"] = windows_run(a)
     if ranks.rank == 0 and not a.no_serve:
         line["serve"] = serve_run(a)
     if ranks.rank == 0 and not a.no_cpu and ranks.world == 1:
@@ -426,6 +430,48 @@ def streamed_run(a, hv) -> dict:
     return {"value": a.n_ind * a.n_snp / t, "unit": UNIT, "ms_per_pass": t * 1e3,
             "h2d_gbs": hv.nbytes / t / 1e9, "block_snps": blk, "blocks": (a.n_snp + blk - 1) // blk,
             "note": "rows in pinned host memory, two device blocks double-buffered on a copy stream"}
+
+
+def windows_run(a) -> dict:
+    """Batched local PCA: 4,096 SNP windows of log-uniform width in [500, 20,000] over a shared
+    2,000-individual Balding-Nichols cohort (K = 4, Fst 0.05, 1% missing), nsv 2, nrhs 8, power 3,
+    the reference's default convergence test (crit 1, tol 1e-3), solved together (dpca_windows_*,
+    mixed precision).  Beside it, a sample of the same windows solved one at a time on their own
+    handles (the first 16 windows)."""
+    import distpca_gb300 as D
+    from distpca_gb300 import synth
+
+    n_ind = 2000
+    widths = synth.window_widths(a.windows, seed=0)
+    c = synth.make_cohort(n_ind, int(widths.sum()), n_pop=4, fst=0.05, missing=0.01, seed=4)
+    flags = dict(nsv=2, power=3)
+    with D.Windows(n_ind, widths, 8) as w:
+        w.synth_fill(c)
+        w.solve(miter=1, want_u=False, **flags)  # warm-up
+        w.reset_kernel_times(True)
+        t0 = time.perf_counter()
+        r = w.solve(want_u=False, **flags)
+        t = time.perf_counter() - t0
+        kt = w.kernel_times()
+    passes = (flags["power"] + 1) * r["its"]
+    gpass = float(np.sum(widths * n_ind * passes))
+    sample = min(16, a.windows)
+    offs = np.concatenate([[0], np.cumsum(widths)])
+    t1 = 0.0
+    for i in range(sample):
+        rows = synth.pack_rows(c, int(offs[i]), int(offs[i + 1]))
+        t0 = time.perf_counter()
+        with D.Handle(n_ind, int(widths[i]), 8, precision="mixed") as h:
+            h.upload(rows)
+            h.solve(D.start_block(n_ind, 8), bsize=int(widths[i]) - 1, **flags)
+        t1 += time.perf_counter() - t0
+    return {"windows": int(a.windows), "n_ind": n_ind, "snps": int(widths.sum()), "nrhs": 8, "nsv": 2, "power": 3,
+            "seconds": t, "windows_per_s": a.windows / t, "genotype_passes_per_s": gpass / t,
+            "its_mean": float(np.mean(r["its"])), "its_max": int(np.max(r["its"])),
+            "kernel_ms": {k: round(v["ms"], 3) for k, v in kt.items()},
+            "one_at_a_time": {"sample": f"the first {sample} windows, one handle each (create, upload, solve)",
+                              "seconds": t1, "windows_per_s": sample / t1},
+            "data": "seeded Balding-Nichols cohort filled on the device"}
 
 
 def serve_run(a) -> dict:

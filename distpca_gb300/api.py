@@ -17,7 +17,7 @@ import numpy as np
 
 __all__ = ["DpcaError", "Config", "Result", "Handle", "lib", "library_path", "config", "parse_args", "probe",
            "resolve", "start_block", "run", "run_packed", "decode_counts", "PREC_FP64", "PREC_MIXED",
-           "exported_symbols", "FullSVD", "full_svd", "Server", "JobInfo", "sym_eig"]
+           "exported_symbols", "FullSVD", "full_svd", "Server", "JobInfo", "sym_eig", "Windows"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PREC_FP64 = 0
@@ -124,6 +124,15 @@ _SIGS = {
                                           ctypes.c_void_p]),
     "dpca_decode_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dpca_windows_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "dpca_windows_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dpca_windows_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "dpca_windows_synth_fill": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_int]),
+    "dpca_windows_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Config), ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]),
+    "dpca_windows_handle": (ctypes.c_void_p, [ctypes.c_void_p]),
     "dpca_serve_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ServeConfig)]),
     "dpca_serve_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_int64)]),
     "dpca_serve_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int),
@@ -513,3 +522,77 @@ class Server:
             self.shutdown()
         except Exception:
             pass
+
+
+class Windows:
+    """Batched local PCA (dpca_windows_*): independent PCAs of consecutive SNP windows that share
+    the individuals, solved together on one GPU.  win_snps[w] SNPs per window, in row order."""
+
+    def __init__(self, n_ind: int, win_snps: Sequence[int], nrhs: int, device: int = 0, stream: Optional[int] = None):
+        self.n_ind, self.nrhs = n_ind, nrhs
+        self.win_snps = np.ascontiguousarray(win_snps, dtype=np.int32)
+        self.n_win = len(self.win_snps)
+        w = ctypes.c_void_p()
+        st = ctypes.c_void_p(stream) if stream else None
+        _check(lib().dpca_windows_create(ctypes.byref(w), n_ind, self.n_win, _p(self.win_snps), nrhs, device, st))
+        self._w = w
+
+    @property
+    def n_snp(self) -> int:
+        return int(self.win_snps.sum())
+
+    def close(self) -> None:
+        if getattr(self, "_w", None):
+            lib().dpca_windows_destroy(self._w)
+            self._w = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, packed: np.ndarray) -> None:
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        assert packed.shape[0] == self.n_snp
+        _check(lib().dpca_windows_upload(self._w, _p(packed), packed.shape[1]))
+
+    def synth_fill(self, cohort) -> None:
+        assert cohort.n_snp == self.n_snp and cohort.n_ind == self.n_ind
+        pop = np.ascontiguousarray(cohort.pop, dtype=np.uint8)
+        miss = np.ascontiguousarray(cohort.miss_thr, dtype=np.uint32)
+        thr = np.ascontiguousarray(cohort.snp_thr, dtype=np.uint32)
+        _check(lib().dpca_windows_synth_fill(self._w, ctypes.c_uint64(cohort.key), _p(pop), _p(miss), _p(thr),
+                                             cohort.n_pop))
+
+    def solve(self, omega0: Optional[np.ndarray] = None, want_u: bool = True, **flags) -> Dict:
+        c = config(nrhs=self.nrhs, **flags)
+        om = None if omega0 is None else np.ascontiguousarray(omega0, dtype=np.float64)
+        sigma = np.zeros((self.n_win, c.nsv))
+        u = np.zeros((self.n_win, self.n_ind, c.nsv)) if want_u else None
+        its = np.zeros(self.n_win, dtype=np.int32)
+        _check(lib().dpca_windows_solve(self._w, ctypes.byref(c), _p(om), _p(sigma), _p(u), _p(its)))
+        return {"sigma": sigma, "u": u, "its": its}
+
+    def handle(self) -> int:
+        return lib().dpca_windows_handle(self._w)
+
+    def kernel_times(self) -> Dict[str, Dict[str, float]]:
+        cap = 64
+        names = ctypes.create_string_buffer(8192)
+        ms = np.zeros(cap)
+        launches = np.zeros(cap, dtype=np.int64)
+        count = ctypes.c_int(0)
+        _check(lib().dpca_kernel_times(ctypes.c_void_p(self.handle()), names, 8192, _p(ms), _p(launches),
+                                       ctypes.byref(count), cap))
+        keys = names.value.decode().split(";") if count.value else []
+        return {k: {"ms": float(ms[i]), "launches": int(launches[i])} for i, k in enumerate(keys)}
+
+    def reset_kernel_times(self, enable: bool = True) -> None:
+        _check(lib().dpca_reset_kernel_times(ctypes.c_void_p(self.handle()), 1 if enable else 0))

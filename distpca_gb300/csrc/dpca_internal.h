@@ -1,6 +1,8 @@
 // Internal declarations shared by the host (.cpp) and device (.cu) parts of libdpca.
 #pragma once
 
+#include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -161,10 +163,11 @@ struct SmallLayout {
 // ---- launchers (device code in .cu files); all stream-ordered on h->stream ----
 dpca_status launch_snp_stats(Handle *h);
 dpca_status launch_synth_fill(Handle *h, uint64_t key, const uint8_t *d_pop, const uint32_t *d_miss,
-                              const uint32_t *d_thr, int n_pop);
+                              const uint32_t *d_thr, int n_pop, const int *d_row_src = nullptr);
 dpca_status launch_transpose_packed(Handle *h);
 void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, double inv_sqrt_nsnp,
-                          int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream);
+                          int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream,
+                          const double *row_inv_sqrt = nullptr);
 void launch_transpose_raw(const uint8_t *P, int64_t pitch, uint8_t *PT, int64_t pitchT, int n_ind, int n_snp,
                           cudaStream_t stream, int s_base = 0);
 // one streamed block: Z (+)= X_b^T (X_b Omega) over SNP rows [s0, s0 + ns) held in buffer b
@@ -183,6 +186,26 @@ dpca_status host_sym_eig_desc(int k, const double *B, double *w, double *W);    
 dpca_status launch_apply_w(Handle *h, const double *q, double *out);                      // out = Q W
 dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol, int ii, const double *old,
                                        const double *omega);
+
+// One mixed pass over W batched windows (k_mixed.cu mixed_win_pass): Z_w = X_w^T X_w Omega_w for
+// every active window, on a mixed handle whose rows are the windows' SNPs, each window padded
+// to whole 512-row blocks (padding rows have zero coefficients).
+struct WinPass {
+    int W = 0;
+    const double *omega = nullptr;  // [W][n][k]
+    double *z = nullptr;            // [W][n][k]
+    const int *tile_win = nullptr;  // [rows / 128] window of each 128-row tile
+    const int *win_kb0 = nullptr, *win_nkb = nullptr;  // [W] 64-SNP K-block range of each window
+    const int *active = nullptr;    // [W] 0 = converged (skipped)
+    __half *omega_s = nullptr;      // [W * 2 kp][n_pad] FP16 slices
+    double *scales = nullptr;       // [W][4][k]
+    unsigned int *colmax = nullptr; // [W][k]
+    long long *colsumq = nullptr, *rq = nullptr;  // [W][k]
+    double *partial = nullptr;      // [W][n][k]
+    CUtensorMap *map_om = nullptr;  // B map over omega_s (built on first use)
+    mutable bool map_ready = false;
+};
+dpca_status mixed_win_pass(Handle *h, const WinPass &p);
 
 // mixed-precision pass (k_mixed.cu)
 dpca_status mixed_prepare(Handle *h);

@@ -95,6 +95,14 @@ struct GemmArgs {
     double *y_out;          // kXW: optional FP64 Y [rows][k]
     double *partial;        // kXTY: [splits][rows][k]
     int *err;
+    // Batched windows (independent problems over consecutive SNP ranges, each padded to whole
+    // 512-SNP K tiles): kXW reads the window of each 128-row tile from tile_win and its Omega
+    // slices from rows [w N, w N + N) of the B map; kXTY runs one K range per blockIdx.y
+    // (win_kb0/win_nkb) and writes partial[w].  scales, colmax and colsumq then hold one block
+    // per window ([4][k], [k], [k]); CTAs of windows whose win_active entry is 0 return at once.
+    const int *tile_win;
+    const int *win_kb0, *win_nkb;
+    const int *win_active;
 };
 
 struct MixedState {
@@ -208,9 +216,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x, split = blockIdx.y;
-    const int kb0 = split * args.kb_per_split;
-    const int nkb = min(args.nkb_total, kb0 + args.kb_per_split) - kb0;
+    const int win = args.tile_win ? args.tile_win[tile] : (args.win_kb0 ? split : 0);
+    if ((args.tile_win || args.win_kb0) && args.win_active && !args.win_active[win]) return;  // whole CTA
+    const int kb0 = args.win_kb0 ? args.win_kb0[split] : split * args.kb_per_split;
+    const int nkb = args.win_kb0 ? args.win_nkb[split] : min(args.nkb_total, kb0 + args.kb_per_split) - kb0;
     const int nb = (nkb + 1) >> 1;  // a trailing half batch reads zero operand columns
+    const int b_row0 = args.tile_win ? win * N : 0;  // first B row of this window's Omega slices
     int *err = args.err;
 
     if (threadIdx.x == 0) {
@@ -261,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 if (!tc::mbar_wait(&free_[r], bph ^ 1, err, 12, true)) break;
                 tc::mbar_arrive_expect_tx(&full[r], bstage);
-                tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, 0, kb0 + 2 * t);
+                tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, b_row0, kb0 + 2 * t);
                 issued_b = t + 1;
                 if (++r == R) r = 0, bph ^= 1;
             }
@@ -396,14 +407,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (j < kp) dst[j * 128] += slices_int(hv[j], lv[j]);
         }
         const bool valid = ok && row < args.rows;
-        const double *sc = args.scales;
+        const double *sc = args.scales + (size_t)win * 4 * k;
+        unsigned int *colmax = args.colmax ? args.colmax + (size_t)win * k : nullptr;
+        const long long *colsumq = args.colsumq ? args.colsumq + (size_t)win * k : nullptr;
         if (MODE == kXW) {
             for (int c = 0; c < k; ++c) {
                 float mag = 0.f;
                 if (valid) {
                     // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum term
                     const double y = ((b - a) * (double)acc[c * 128 + r] +
-                                      a * (double)(acc[(kp + c) * 128 + r] + args.colsumq[c])) *
+                                      a * (double)(acc[(kp + c) * 128 + r] + colsumq[c])) *
                                      sc[k + c];
                     if (args.y_out) args.y_out[(size_t)row * k + c] = y;
                     args.yt[(int64_t)c * args.yt_ld + row] = (float)y;
@@ -411,7 +424,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
-                if (lane == 0 && mag > 0.f) atomicMax(args.colmax + c, __float_as_uint(mag));
+                if (lane == 0 && mag > 0.f) atomicMax(colmax + c, __float_as_uint(mag));
             }
         } else if (valid) {
             double *out = args.partial + ((size_t)split * args.rows + row) * k;
@@ -541,6 +554,114 @@ __global__ void reduce_parts_kernel(const double *__restrict__ partial, int64_t 
     }
 }
 
+// ------------------------------------------------------------------ batched windows
+// The same operand preparation for W independent problems at once (one per SNP window): Omega_w
+// is om_all[w] (n x k), its slices go to rows [w N, w N + N) of out, scales/colsumq/rq hold one
+// block per window.  Inactive windows (active[w] == 0) are skipped.
+__global__ void __launch_bounds__(256) win_omega_split_kernel(const double *__restrict__ om_all, int n, int k,
+                                                              int kp, int n_pad, int N, double *__restrict__ scales_w,
+                                                              __half *__restrict__ out, long long *__restrict__ colsumq_w,
+                                                              const int *__restrict__ active) {
+    __shared__ double redm[32];
+    __shared__ double scs[kMaxMixedNrhs];
+    __shared__ long long sums[kMaxMixedNrhs];
+    const int w = blockIdx.x;
+    if (active && !active[w]) return;
+    const double *om = om_all + (size_t)w * n * k;
+    for (int c = 0; c < k; ++c) {
+        double mx = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, fabs(om[(size_t)i * k + c]));
+        mx = warp_max(mx);
+        if ((threadIdx.x & 31) == 0) redm[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) mx = fmax(mx, redm[q]);
+            const double so = pow2_scale_below(mx);
+            scs[c] = so;
+            sums[c] = 0;
+            scales_w[(size_t)w * 4 * k + c] = so;
+            scales_w[(size_t)w * 4 * k + k + c] = 1.0 / so;
+        }
+        __syncthreads();
+    }
+    __half *o = out + (size_t)w * N * n_pad;
+    for (int c = 0; c < kp; ++c) {
+        long long part = 0;
+        for (int i = threadIdx.x; i < n_pad; i += blockDim.x) {
+            const int src = (i & ~15) | perm16(i & 15);
+            __half hi = __float2half(0.f), lo = __float2half(0.f);
+            if (c < k && src < n) {
+                const double v = om[(size_t)src * k + c] * scs[c];
+                part += (long long)rint(v);
+                fixed_slices(v, hi, lo);
+            }
+            o[(size_t)c * n_pad + i] = hi;
+            o[(size_t)(kp + c) * n_pad + i] = lo;
+        }
+        if (c < k && part != 0) atomicAdd((unsigned long long *)(sums + c), (unsigned long long)part);
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < k; c += blockDim.x) colsumq_w[(size_t)w * k + c] = sums[c];
+}
+
+// The a.Y, (b-a).Y scales of every window from its exact column maxima.
+__global__ void win_bop_scales_kernel(const unsigned int *__restrict__ colmax_w, int W, int k,
+                                      double *__restrict__ scales_w, const int *__restrict__ active) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < W * k; e += gridDim.x * blockDim.x) {
+        const int w = e / k, c = e - w * k;
+        if (active && !active[w]) continue;
+        const double sc = pow2_scale_below((double)__uint_as_float(colmax_w[e]) * 1.001);
+        scales_w[(size_t)w * 4 * k + 2 * k + c] = sc;
+        scales_w[(size_t)w * 4 * k + 3 * k + c] = 1.0 / sc;
+    }
+}
+
+// bop_split_kernel over all window rows: the window of row s is tile_win[s / 128] (windows are
+// whole 512-row blocks, so a warp's 32 rows and a 16-row permutation group share one window).
+__global__ void __launch_bounds__(256) win_bop_split_kernel(const float *__restrict__ yt, int64_t ld, int rows, int k,
+                                                            int kp, int N, const double *__restrict__ coef,
+                                                            const int *__restrict__ tile_win,
+                                                            const double *__restrict__ scales_w,
+                                                            __half *__restrict__ bop, long long *__restrict__ rq_w,
+                                                            const int *__restrict__ active) {
+    const int n128 = (rows + 127) & ~127;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n128; s += gridDim.x * blockDim.x) {
+        const int w = tile_win[s >> 7];
+        if (active && !active[w]) continue;  // warp-uniform
+        const double *sw = scales_w + (size_t)w * 4 * k;
+        const int src = (s & ~15) | perm16(s & 15);
+        const bool valid = src < rows;
+        const float b = valid ? (float)coef[2 * (size_t)src] : 0.f;
+        const float a = valid ? (float)coef[2 * (size_t)src + 1] : 0.f;
+        const float bma = b - a;
+        for (int c = 0; c < k; ++c) {
+            const float y = valid ? yt[(int64_t)c * ld + src] * (float)sw[2 * k + c] : 0.f;
+            const int n1 = __float2int_rn(a * y), n2 = __float2int_rn(bma * y);
+            const int h1 = (n1 + 2048) >> 12, h2 = (n2 + 2048) >> 12;
+            bop[(int64_t)c * ld + s] = __int2half_rn(h2);
+            bop[(int64_t)(kp + c) * ld + s] = __int2half_rn(n2 - (h2 << 12));
+            bop[(int64_t)(N + c) * ld + s] = __int2half_rn(h1);
+            bop[(int64_t)(N + kp + c) * ld + s] = __int2half_rn(n1 - (h1 << 12));
+            const int ws = __reduce_add_sync(0xffffffffu, n1);
+            if ((threadIdx.x & 31) == 0 && ws != 0)
+                atomicAdd((unsigned long long *)(rq_w + (size_t)w * k + c), (unsigned long long)(long long)ws);
+        }
+    }
+}
+
+// z_w[i][c] = partial_w[i][c] + rq_w[c] / scale_w[c] (one K range per window: no split sum).
+__global__ void win_reduce_kernel(const double *__restrict__ partial, int W, int n, int k,
+                                  const long long *__restrict__ rq_w, const double *__restrict__ scales_w,
+                                  double *__restrict__ z, const int *__restrict__ active) {
+    const int64_t per = (int64_t)n * k, total = per * W;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int w = (int)(e / per);
+        if (active && !active[w]) continue;
+        const int c = (int)(e % k);
+        z[e] = partial[e] + (double)rq_w[(size_t)w * k + c] * scales_w[(size_t)w * 4 * k + 3 * k + c];
+    }
+}
+
 // ------------------------------------------------------------------ host side
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -582,7 +703,9 @@ static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base
 
 // FP16 slice operand [rows][n_pad] seen as [K-block][rows][64]: one box = one batch of two
 // K-blocks, each a rows x 128 B tile (n_pad is a multiple of 128, so whole batches exist).
-static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, uint64_t rows) {
+// FP16 operand [rows][n_pad] as 3-D boxes of box_rows rows x 2 K-blocks of 64 (box_rows = rows,
+// or the N rows of one window when the rows stack several windows' slices).
+static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, uint64_t rows, uint32_t box_rows = 0) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) {
         set_error("cuTensorMapEncodeTiled unavailable");
@@ -590,7 +713,7 @@ static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, 
     }
     cuuint64_t dims[3] = {64, rows, n_pad / 64};
     cuuint64_t strides[2] = {n_pad * 2, 128};
-    cuuint32_t box[3] = {64, (cuuint32_t)rows, 2};
+    cuuint32_t box[3] = {64, box_rows ? box_rows : (cuuint32_t)rows, 2};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -805,6 +928,86 @@ static dpca_status xty_rows(Handle *h, const CUtensorMap &map_a, int nsnp, doubl
     reduce_parts_kernel<<<grid, 256, 0, h->stream>>>(m->partial, elems, splits, k, m->rq, m->scales + 3 * k, z,
                                                      accumulate ? 1 : 0);
     DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
+// ---- batched windows: one pass over all active windows (see the GemmArgs window fields) ----
+dpca_status mixed_win_pass(Handle *h, const WinPass &p) {
+    MixedState *m = mstate(h);
+    const int k = h->k, kp = m->kp, N = m->N, n = h->n_ind;
+    const int rows = h->n_snp, rows_pad = (rows + 127) / 128 * 128;
+    if (!p.map_ready) {
+        DPCA_TRY(make_batch_map(p.map_om, p.omega_s, h->n_ind_pad, (uint64_t)p.W * N, (uint32_t)N));
+        p.map_ready = true;
+    }
+    {
+        ScopedLaunch t(&h->clock, h->stream, "win_split_omega");
+        win_omega_split_kernel<<<p.W, 256, 0, h->stream>>>(p.omega, n, k, kp, h->n_ind_pad, N, p.scales, p.omega_s,
+                                                           p.colsumq, p.active);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    DPCA_CUDA(cudaMemsetAsync(p.colmax, 0, (size_t)p.W * k * 4, h->stream));
+    DPCA_CUDA(cudaMemsetAsync(p.rq, 0, (size_t)p.W * k * 8, h->stream));
+    GemmArgs a{};
+    a.rows = rows;
+    a.nkb_total = ceil_div(n, 64);
+    a.kb_per_split = 8 * ceil_div(a.nkb_total, 8);
+    a.k = k;
+    a.kp = kp;
+    a.N = N;
+    a.ring = m->ring1;
+    a.coef = h->coef;
+    a.scales = p.scales;
+    a.yt = m->yt;
+    a.yt_ld = rows_pad;
+    a.colmax = p.colmax;
+    a.colsumq = p.colsumq;
+    a.err = h->dflag;
+    a.tile_win = p.tile_win;
+    a.win_active = p.active;
+    {
+        ScopedLaunch t(&h->clock, h->stream, "win_mixed_xw");
+        mixed_gemm_kernel<kXW><<<dim3(ceil_div(rows, 128), 1), kThreads, m->smem1, h->stream>>>(m->map_p[0], *p.map_om,
+                                                                                                 a);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    {
+        ScopedLaunch t(&h->clock, h->stream, "win_split_bop");
+        win_bop_scales_kernel<<<ceil_div(p.W * k, 256), 256, 0, h->stream>>>(p.colmax, p.W, k, p.scales, p.active);
+        DPCA_CUDA(cudaGetLastError());
+        const int grid = std::min(ceil_div(rows_pad, 256), h->sm_count * 8);
+        win_bop_split_kernel<<<grid, 256, 0, h->stream>>>(m->yt, rows_pad, rows, k, kp, N, h->coef, p.tile_win,
+                                                           p.scales, m->bop, p.rq, p.active);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    GemmArgs b{};
+    b.rows = n;
+    b.a_ktiles = (int)(h->pitchT / 128);
+    b.nkb_total = ceil_div(rows, 64);
+    b.kb_per_split = 8;
+    b.k = k;
+    b.kp = kp;
+    b.N = N;
+    b.ring = m->ring2;
+    b.scales = p.scales;
+    b.partial = p.partial;
+    b.err = h->dflag;
+    b.win_kb0 = p.win_kb0;
+    b.win_nkb = p.win_nkb;
+    b.win_active = p.active;
+    {
+        ScopedLaunch t(&h->clock, h->stream, "win_mixed_xty");
+        mixed_gemm_kernel<kXTY><<<dim3(ceil_div(n, 128), p.W), kThreads, m->smem2, h->stream>>>(m->map_pt[0],
+                                                                                                 m->map_bop, b);
+        DPCA_CUDA(cudaGetLastError());
+    }
+    {
+        ScopedLaunch t(&h->clock, h->stream, "win_reduce");
+        const int64_t total = (int64_t)p.W * n * k;
+        const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 8);
+        win_reduce_kernel<<<grid, 256, 0, h->stream>>>(p.partial, p.W, n, k, p.rq, p.scales, p.z, p.active);
+        DPCA_CUDA(cudaGetLastError());
+    }
     return DPCA_OK;
 }
 

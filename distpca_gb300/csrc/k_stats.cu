@@ -64,12 +64,16 @@ __global__ void __launch_bounds__(256) snp_counts_kernel(const uint8_t *__restri
 }
 
 // Pass 2: one thread per SNP turns its counts into mean, sd, the LUT and the mixed-path
-// coefficients (the FP64 divisions stay off the streaming pass).
-__global__ void __launch_bounds__(256) snp_moments_kernel(int n_snp, double inv_sqrt_nsnp,
+// coefficients (the FP64 divisions stay off the streaming pass).  row_inv_sqrt (optional) gives
+// each row its own 1/sqrt(n_snp): batched windows standardize each window on its own, and a
+// padding row gets 0 (zero LUT and coefficients).
+__global__ void __launch_bounds__(256) snp_moments_kernel(int n_snp, double inv_sqrt_all,
                                                           const int32_t *__restrict__ counts, double *__restrict__ avg,
                                                           double *__restrict__ sd, double *__restrict__ lut,
-                                                          double *__restrict__ coef) {
+                                                          double *__restrict__ coef,
+                                                          const double *__restrict__ row_inv_sqrt) {
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_snp; s += (int64_t)gridDim.x * blockDim.x) {
+        const double inv_sqrt_nsnp = row_inv_sqrt ? row_inv_sqrt[s] : inv_sqrt_all;
         const int c00 = counts[4 * s + 0], c10 = counts[4 * s + 2], c11 = counts[4 * s + 3];
         double sum = (double)c10 + 2.0 * (double)c11;  // exact: small integers
         unsigned int ctr = (unsigned int)(c00 + c10 + c11);
@@ -109,26 +113,34 @@ dpca_status launch_snp_stats(Handle *h) {
 // streaming sweep, whose rows are one block of the matrix (inv_sqrt_nsnp is then the whole
 // matrix's 1/sqrt(n_snp)).
 void launch_snp_stats_raw(const uint8_t *P, int64_t pitch, int n_ind, int n_snp, double inv_sqrt_nsnp,
-                          int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream) {
+                          int32_t *counts, double *avg, double *sd, double *lut, double *coef, cudaStream_t stream,
+                          const double *row_inv_sqrt) {
     const int64_t np = ((int64_t)n_ind + 3) / 4;
     snp_counts_kernel<<<ceil_div(n_snp, 8), 256, 0, stream>>>(P, pitch, n_ind, n_snp, np, counts);
     snp_moments_kernel<<<std::min(ceil_div(n_snp, 256), 4096), 256, 0, stream>>>(n_snp, inv_sqrt_nsnp, counts, avg,
-                                                                                  sd, lut, coef);
+                                                                                  sd, lut, coef, row_inv_sqrt);
 }
 
 // One thread writes one 32-bit word (16 individuals) of one SNP row; the
 // genotype of (snp s, individual i) is a pure function of (key, s, i), as in
 // distpca_gb300/synth.py::genotype_codes.
+// row_src (optional): the cohort SNP drawn into each device row, -1 for a padding row (zero codes).
 __global__ void __launch_bounds__(256) synth_fill_kernel(uint8_t *__restrict__ P, int64_t pitch, int n_ind,
                                                          int n_snp, int64_t words_per_row, uint64_t key,
                                                          const uint8_t *__restrict__ pop,
                                                          const uint32_t *__restrict__ miss_thr,
-                                                         const uint32_t *__restrict__ thr, int n_pop) {
+                                                         const uint32_t *__restrict__ thr, int n_pop,
+                                                         const int *__restrict__ row_src) {
     int64_t total = words_per_row * (int64_t)n_snp;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t s = t / words_per_row;
-        int64_t w = t - s * words_per_row;
+        const int64_t row = t / words_per_row;
+        int64_t w = t - row * words_per_row;
+        const int64_t s = row_src ? (int64_t)row_src[row] : row;
+        if (s < 0) {
+            *reinterpret_cast<uint32_t *>(P + row * pitch + 4 * w) = 0u;
+            continue;
+        }
         const uint32_t *ts = thr + s * n_pop;
         uint32_t word = 0;
 #pragma unroll 4
@@ -144,17 +156,17 @@ __global__ void __launch_bounds__(256) synth_fill_kernel(uint8_t *__restrict__ P
             if ((uint32_t)hm < __ldg(miss_thr + i)) code = 1u;
             word |= code << (2 * j);
         }
-        *reinterpret_cast<uint32_t *>(P + s * pitch + 4 * w) = word;
+        *reinterpret_cast<uint32_t *>(P + row * pitch + 4 * w) = word;
     }
 }
 
 dpca_status launch_synth_fill(Handle *h, uint64_t key, const uint8_t *d_pop, const uint32_t *d_miss,
-                              const uint32_t *d_thr, int n_pop) {
+                              const uint32_t *d_thr, int n_pop, const int *d_row_src) {
     int64_t wpr = (h->np + 3) / 4;
     int64_t total = wpr * h->n_snp;
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 32);
     synth_fill_kernel<<<grid, 256, 0, h->stream>>>(h->P, h->pitch, h->n_ind, h->n_snp, wpr, key, d_pop, d_miss,
-                                                    d_thr, n_pop);
+                                                    d_thr, n_pop, d_row_src);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -170,7 +182,9 @@ __global__ void __launch_bounds__(256) transpose_packed_kernel(const uint8_t *__
                                                                uint8_t *__restrict__ PT, int64_t pitchT, int n_ind,
                                                                int n_snp, int s_base) {
     __shared__ uint8_t codes[kTS][kTI + 4];
-    int s0 = blockIdx.y * kTS, i0 = blockIdx.x * kTI;
+    // SNP blocks on grid x (up to 2^31 - 1), individual blocks on y: matrices of more than
+    // 65,535 SNP blocks stay launchable
+    int s0 = blockIdx.x * kTS, i0 = blockIdx.y * kTI;
     int tid = threadIdx.x;
     // load: 64 rows x 64 bytes; thread -> (row, 16-byte chunk): 256 threads = 64 rows x 4 chunks
     {
@@ -213,13 +227,13 @@ __global__ void __launch_bounds__(256) transpose_packed_kernel(const uint8_t *__
 // Rows [0, n_snp) of P are SNPs s_base + [0, n_snp) of PT (s_base a multiple of 64).
 void launch_transpose_raw(const uint8_t *P, int64_t pitch, uint8_t *PT, int64_t pitchT, int n_ind, int n_snp,
                           cudaStream_t stream, int s_base) {
-    dim3 grid(ceil_div(n_ind, kTI), ceil_div(n_snp, kTS));
+    dim3 grid(ceil_div(n_snp, kTS), ceil_div(n_ind, kTI));
     transpose_packed_kernel<<<grid, 256, 0, stream>>>(P, pitch, PT, pitchT, n_ind, n_snp, s_base);
 }
 
 dpca_status launch_transpose_packed(Handle *h) {
     ScopedLaunch t(&h->clock, h->stream, "transpose_packed");
-    dim3 grid(ceil_div(h->n_ind, kTI), ceil_div(h->n_snp, kTS));
+    dim3 grid(ceil_div(h->n_snp, kTS), ceil_div(h->n_ind, kTI));
     transpose_packed_kernel<<<grid, 256, 0, h->stream>>>(h->P, h->pitch, h->PT, h->pitchT, h->n_ind, h->n_snp, 0);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;

@@ -227,3 +227,9 @@ def serve_cohort(job: dict) -> Cohort:
     """The cohort tables of one serve_stream job."""
     return make_cohort(job["n_ind"], job["n_snp"], n_pop=job["n_pop"], fst=job["fst"], missing=job["missing"],
                        seed=job["seed"])
+
+
+def window_widths(n_win: int = 4096, lo: int = 500, hi: int = 20000, seed: int = 0) -> np.ndarray:
+    """SNP widths of n_win consecutive windows, log-uniform in [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    return np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_win))).astype(np.int64)

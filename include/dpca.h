@@ -218,6 +218,31 @@ dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_
 dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp,
                                    const double *omega, int nrhs, double *z, void *stream);
 
+/* ---- batched local PCA over SNP windows ----
+ * The reference runs one PCA per invocation (src/distpca.cpp:83-405).  A dpca_windows object
+ * holds W independent PCA problems that share the individuals: window w is the next win_snps[w]
+ * SNP rows of one packed matrix (consecutive windows, sum(win_snps) rows), standardized on its
+ * own (1/sqrt(win_snps[w]) in place of 1/sqrt(n_snp), src/utilities.cpp:294-305).  dpca_windows_solve
+ * runs the subspace iteration of dpca_solve on every window at once -- mixed precision, a full
+ * pass for the Rayleigh quotient (bsize < n_snp) -- with one launch of each kernel per step for
+ * all windows still iterating; a window stops at its own convergence test (cfg->crit, tol,
+ * miter) and keeps its result.  nrhs <= 48, at most 65,535 windows. */
+typedef struct dpca_windows dpca_windows;
+dpca_status dpca_windows_create(dpca_windows **w, int n_ind, int n_win, const int *win_snps, int nrhs, int device,
+                                void *stream);
+dpca_status dpca_windows_destroy(dpca_windows *w);
+/* Packed host rows of all windows in order (row_stride >= ceil(n_ind/4) bytes apart). */
+dpca_status dpca_windows_upload(dpca_windows *w, const uint8_t *packed, int64_t row_stride);
+/* A seeded Balding-Nichols cohort over sum(win_snps) SNPs (the dpca_synth_fill tables). */
+dpca_status dpca_windows_synth_fill(dpca_windows *w, uint64_t key, const uint8_t *pop, const uint32_t *miss_thr,
+                                    const uint32_t *snp_thr, int n_pop);
+/* omega0: n_ind x nrhs start block for every window (NULL: dpca_start_block's).  Outputs:
+ * sigma[n_win * nsv]; u[n_win * n_ind * nsv] or NULL; its[n_win] outer iterations or NULL. */
+dpca_status dpca_windows_solve(dpca_windows *w, const dpca_config *cfg, const double *omega0, double *sigma,
+                               double *u, int *its);
+/* The handle the windows run on, for dpca_kernel_times / dpca_reset_kernel_times. */
+dpca_handle *dpca_windows_handle(dpca_windows *w);
+
 /* ---- serving loop: many independent PCA jobs on one GPU ----
  * The reference runs one PCA per MPI job: main reads one .bed and calls the solver once
  * (src/distpca.cpp:83-405 -> BlockSubspaceIter_MPI_OOC_double_buffering, src/methods.h:49).

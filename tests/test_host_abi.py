@@ -234,3 +234,13 @@ def test_sym_eig_matches_numpy(dpca, k):
         np.testing.assert_allclose(w, ref, atol=1e-12 * scale, rtol=0)
         np.testing.assert_allclose(W.T @ W, np.eye(k), atol=1e-12)
         assert np.abs(a @ W - W * w).max() <= 1e-12 * scale
+
+
+def test_windows_reject_bad_shapes_before_the_device(dpca):
+    # checked before any device work, so these hold without a GPU too
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.Windows(500, [1000, 0, 10], 8)
+    assert e.value.status == 1
+    with pytest.raises(dpca.DpcaError) as e:
+        dpca.Windows(500, [1000], 64)
+    assert e.value.status == 6
