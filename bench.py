@@ -386,6 +386,7 @@ def e2e_run(a, hv) -> dict:
               precision=a.precision)
     om0 = D.start_block(a.n_ind, a.nrhs)
     D.run_packed(hv, a.n_ind, omega0=om0, **kw)  # warm-up (context, allocator)
+    link = host_link_gbs(hv)
     times, passes = [], 0
     for _ in range(a.e2e_steps):
         t0 = time.perf_counter()
@@ -397,7 +398,30 @@ def e2e_run(a, hv) -> dict:
             "h2d_bytes_per_step": int(hv.nbytes + a.n_ind * a.nrhs * 8),
             "d2h_bytes_per_step": int(a.n_ind * a.nrhs * 8),
             "call": f"dpca_run_packed, 1 outer iteration = {passes} passes incl. H2D, stats, QR, Rayleigh-Ritz",
-            "seconds_per_call": t}
+            "seconds_per_call": t,
+            "host_link_gbs": link,
+            "note": "the 12.5 GB host-to-device copy is part of each call; host_link_gbs is a plain pinned copy "
+                    "measured just before (the host link is shared on this machine and varies between runs)"}
+
+
+def host_link_gbs(hv) -> float:
+    """Pinned host-to-device bandwidth of a plain 2 GB copy from the bench's host buffer."""
+    import torch
+
+    nbytes = min(hv.nbytes, 2_000_000_000)
+    src = torch.from_numpy(hv.reshape(-1)[:nbytes])
+    dst = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    dst.copy_(src, non_blocking=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        dst.copy_(src, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    del dst
+    torch.cuda.empty_cache()
+    return 3 * nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9
 
 
 def streamed_run(a, hv) -> dict:
