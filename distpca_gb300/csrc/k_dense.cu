@@ -413,11 +413,18 @@ __global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__
                                                                 int always_shift, double *__restrict__ Rinv) {
     extern __shared__ double g[];  // k x k, upper triangle -> R
     __shared__ double sh_inv[kMaxNrhs];
+    __shared__ double sh_shift;
     __shared__ int broke;
     const int tid = threadIdx.x;
-    double tr = 0.0;
-    for (int i = 0; i < k; ++i) tr += G[(size_t)i * k + i];  // every thread: same order, same value
-    const double shift = 11.0 * ((double)n * k + (double)k * (k + 1)) * 0x1p-53 * tr;
+    // FP64 is a small fraction of this GPU's arithmetic: scalar work (trace, pivots) is done once
+    // by thread 0 and broadcast through shared memory
+    if (tid == 0) {
+        double tr = 0.0;
+        for (int i = 0; i < k; ++i) tr += G[(size_t)i * k + i];
+        sh_shift = 11.0 * ((double)n * k + (double)k * (k + 1)) * 0x1p-53 * tr;
+    }
+    __syncthreads();
+    const double shift = sh_shift;
     for (int attempt = always_shift ? 1 : 0; attempt < 2; ++attempt) {
         for (int e = tid; e < k * k; e += kCholThreads) {
             const int i = e / k, c = e - i * k;
@@ -427,17 +434,18 @@ __global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__
         __syncthreads();
         const int tx = tid & 15, ty = tid >> 4;  // 16 x 16 map of the trailing block
         for (int j = 0; j < k; ++j) {
-            // every thread reads the pivot and scales its share of row j by 1/sqrt(pivot)
-            double d = g[(size_t)j * k + j];
-            const bool bad = !(d > 0.0) || !isfinite(d);
-            if (bad) d = 1.0;
-            const double inv = rsqrt(d);
-            __syncthreads();  // everyone has read the pivot
             if (tid == 0) {
-                if (bad) broke = 1;
+                double d = g[(size_t)j * k + j];
+                if (!(d > 0.0) || !isfinite(d)) {
+                    broke = 1;
+                    d = 1.0;
+                }
+                const double inv = rsqrt(d);
                 g[(size_t)j * k + j] = d * inv;
                 sh_inv[j] = inv;
             }
+            __syncthreads();
+            const double inv = sh_inv[j];
             for (int c = j + 1 + tid; c < k; c += kCholThreads) g[(size_t)j * k + c] *= inv;
             __syncthreads();
             // trailing update of the upper triangle: g[a][b] -= r[j][a] r[j][b], j < a <= b
