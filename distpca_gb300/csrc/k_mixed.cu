@@ -103,6 +103,7 @@ struct GemmArgs {
     const int *tile_win;
     const int *win_kb0, *win_nkb;
     const int *win_active;
+    int tiles, items;  // work items = tiles x splits (tile fastest); the grid is one CTA per SM at most
 };
 
 struct MixedState {
@@ -192,6 +193,25 @@ __device__ __forceinline__ int chunk_end(int c, int nb, int first, int len) {
     return min(first - 1 + c * len, nb - 1);
 }
 
+// Work item `it` of a launch: tile it % tiles, split it / tiles (for batched windows, the window
+// of the tile or the split); nb = 0 for a window that has converged.  Every role of a CTA
+// evaluates the same items in the same order.
+struct WorkItem {
+    int tile, split, win, kb0, nb;
+};
+
+__device__ __forceinline__ WorkItem work_item(const GemmArgs &a, int it) {
+    WorkItem x;
+    x.tile = it % a.tiles;
+    x.split = it / a.tiles;
+    x.win = a.tile_win ? a.tile_win[x.tile] : (a.win_kb0 ? x.split : 0);
+    const bool skip = (a.tile_win || a.win_kb0) && a.win_active && !a.win_active[x.win];
+    x.kb0 = a.win_kb0 ? a.win_kb0[x.split] : x.split * a.kb_per_split;
+    const int nkb = a.win_kb0 ? a.win_nkb[x.split] : min(a.nkb_total, x.kb0 + a.kb_per_split) - x.kb0;
+    x.nb = skip ? 0 : (nkb + 1) >> 1;  // a trailing half batch reads zero operand columns
+    return x;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     mixed_gemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
@@ -215,22 +235,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tile = blockIdx.x, split = blockIdx.y;
-    const int win = args.tile_win ? args.tile_win[tile] : (args.win_kb0 ? split : 0);
-    if ((args.tile_win || args.win_kb0) && args.win_active && !args.win_active[win]) return;  // whole CTA
-    const int kb0 = args.win_kb0 ? args.win_kb0[split] : split * args.kb_per_split;
-    const int nkb = args.win_kb0 ? args.win_nkb[split] : min(args.nkb_total, kb0 + args.kb_per_split) - kb0;
-    const int nb = (nkb + 1) >> 1;  // a trailing half batch reads zero operand columns
-    const int b_row0 = args.tile_win ? win * N : 0;  // first B row of this window's Omega slices
     int *err = args.err;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kPStages; ++s) {
             tc::mbar_init(&pk_full[s], 1);
-            tc::mbar_init(&pk_empty[s], 4 * kDecodeGroups);  // one elected lane per decode warp
+            tc::mbar_init(&pk_empty[s], 4 * kDecodeGroups);  // every decode warp releases every stage
         }
         for (int s = 0; s < R; ++s) {
-            tc::mbar_init(&full[s], 1 + 4);  // producer (with the TMA bytes) + 4 decode warps
+            tc::mbar_init(&full[s], 1 + 4);  // producer (with the TMA bytes) + the group's 4 decode warps
             tc::mbar_init(&free_[s], 2);     // one commit per MMA issuer
         }
         for (int v = 0; v < 2; ++v) {
@@ -252,29 +265,38 @@ __global__ void __launch_bounds__(kThreads, 1)
     // TMEM columns: G' accumulator [0, N), M accumulator [N, 2N) (each [h | l] slices), then
     // the two A stages (decode group g owns [a_base + 128 g, +128): G' K-blocks 0-1, then M).
     const int a_base = (2 * N + 31) & ~31;
+    // Persistent CTA: items blockIdx.x, blockIdx.x + gridDim.x, ... in order.  Every role walks
+    // the same items; ring slots, barrier phases, A stages (global batch parity) and chunk
+    // parities run on across items, so one item's pipeline fill and epilogue overlap the next.
 
     if (warp == 0) {
         // ---------------------------------------------------------- TMA producer
         if (lane == 0) {
             int sp = 0, r = 0, issued_p = 0, issued_b = 0;
             uint32_t pph = 0, bph = 0;
-            for (int t = 0; t < nb; ++t) {
-                if ((t & 3) == 0) {
-                    if (!tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true)) break;
-                    tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
-                    if (MODE == kXTY)  // tile-blocked: tile (row block, K tile) at row ((rb * nkt) + kt) * 128
-                        tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], 0,
-                                        (tile * args.a_ktiles + ((kb0 + 2 * t) >> 3)) * 128);
-                    else
-                        tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (kb0 + 2 * t) * 16, tile * 128);
-                    issued_p = (t >> 2) + 1;
-                    if (++sp == kPStages) sp = 0, pph ^= 1;
+            bool ok = true;
+            for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
+                const WorkItem x = work_item(args, it);
+                const int b_row0 = args.tile_win ? x.win * N : 0;  // this window's Omega slices
+                for (int t = 0; t < x.nb; ++t) {
+                    if ((t & 3) == 0) {
+                        if (!(ok = tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true))) break;
+                        tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
+                        if (MODE == kXTY)  // tile-blocked: (row block, K tile) at row ((rb * nkt) + kt) * 128
+                            tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], 0,
+                                            (x.tile * args.a_ktiles + ((x.kb0 + 2 * t) >> 3)) * 128);
+                        else
+                            tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (x.kb0 + 2 * t) * 16,
+                                            x.tile * 128);
+                        ++issued_p;
+                        if (++sp == kPStages) sp = 0, pph ^= 1;
+                    }
+                    if (!(ok = tc::mbar_wait(&free_[r], bph ^ 1, err, 12, true))) break;
+                    tc::mbar_arrive_expect_tx(&full[r], bstage);
+                    tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, b_row0, x.kb0 + 2 * t);
+                    ++issued_b;
+                    if (++r == R) r = 0, bph ^= 1;
                 }
-                if (!tc::mbar_wait(&free_[r], bph ^ 1, err, 12, true)) break;
-                tc::mbar_arrive_expect_tx(&full[r], bstage);
-                tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, b_row0, kb0 + 2 * t);
-                issued_b = t + 1;
-                if (++r == R) r = 0, bph ^= 1;
             }
             // drain: every issued copy must land before the CTA may exit
             for (int g = max(0, issued_p - kPStages); g < issued_p; ++g)
@@ -295,140 +317,168 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t tile_units = (uint64_t)(tile_bytes >> 4);
             const uint32_t d = tbase + (uint32_t)(v * N);
             const uint32_t a_v = tbase + (uint32_t)(a_base + 64 * v);
-            int r = 0, left = first_len, chunk = 0;
-            uint32_t ph = 0;
-            bool fresh = true;
-            for (int t = 0; t < nb; ++t) {
-                if (!wait_fast(&full[r], ph, err, 21)) break;
-                if (fresh && chunk > 0 && !wait_fast(&acc_empty[v], (chunk - 1) & 1, err, 22)) break;
-                tc::fence_after_sync();
-                const uint64_t b1 = bdesc0 + (uint64_t)((r * bstage) >> 4), b2 = b1 + tile_units;
-                const uint32_t a = a_v + (uint32_t)(128 * (t & 1));
-                tc::mma_ts_f16(d, a, b1, idesc, fresh ? 0u : 1u);
-                tc::mma_ts_f16(d, a + 8, b1 + 2, idesc, 1u);
-                tc::mma_ts_f16(d, a + 16, b1 + 4, idesc, 1u);
-                tc::mma_ts_f16(d, a + 24, b1 + 6, idesc, 1u);
-                tc::mma_ts_f16(d, a + 32, b2, idesc, 1u);
-                tc::mma_ts_f16(d, a + 40, b2 + 2, idesc, 1u);
-                tc::mma_ts_f16(d, a + 48, b2 + 4, idesc, 1u);
-                tc::mma_ts_f16(d, a + 56, b2 + 6, idesc, 1u);
-                tc::mma_commit(&free_[r]);
-                fresh = false;
-                if (--left == 0 || t == nb - 1) {
-                    tc::mma_commit(&acc_full[v]);
-                    ++chunk;
-                    left = len;
-                    fresh = true;
+            int r = 0, cv = 0;  // B ring slot; chunks of this accumulator committed (all items)
+            uint32_t ph = 0, stage = 0;  // stage = global batch parity
+            bool ok = true;
+            for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
+                const int nb = work_item(args, it).nb;
+                int left = first_len;
+                bool fresh = true;
+                for (int t = 0; t < nb; ++t) {
+                    if (!(ok = wait_fast(&full[r], ph, err, 21))) break;
+                    if (fresh && cv > 0 && !(ok = wait_fast(&acc_empty[v], (cv - 1) & 1, err, 22))) break;
+                    tc::fence_after_sync();
+                    const uint64_t b1 = bdesc0 + (uint64_t)((r * bstage) >> 4), b2 = b1 + tile_units;
+                    const uint32_t a = a_v + 128u * stage;
+                    tc::mma_ts_f16(d, a, b1, idesc, fresh ? 0u : 1u);
+                    tc::mma_ts_f16(d, a + 8, b1 + 2, idesc, 1u);
+                    tc::mma_ts_f16(d, a + 16, b1 + 4, idesc, 1u);
+                    tc::mma_ts_f16(d, a + 24, b1 + 6, idesc, 1u);
+                    tc::mma_ts_f16(d, a + 32, b2, idesc, 1u);
+                    tc::mma_ts_f16(d, a + 40, b2 + 2, idesc, 1u);
+                    tc::mma_ts_f16(d, a + 48, b2 + 4, idesc, 1u);
+                    tc::mma_ts_f16(d, a + 56, b2 + 6, idesc, 1u);
+                    tc::mma_commit(&free_[r]);
+                    fresh = false;
+                    if (--left == 0 || t == nb - 1) {
+                        tc::mma_commit(&acc_full[v]);
+                        ++cv;
+                        left = len;
+                        fresh = true;
+                    }
+                    if (++r == R) r = 0, ph ^= 1;
+                    stage ^= 1u;
                 }
-                if (++r == R) r = 0, ph ^= 1;
             }
         }
     } else if (warp >= 2 && warp < 2 + 4 * kDecodeGroups) {
         // ---------------------------------------------------------- decode (warps 2..9)
+        // Group grp decodes the batches of odd/even global index (its A stage).  Every group
+        // waits for and releases every packed stage, also one holding none of its batches, so
+        // a stage's release count is the same for any item length.
         const int grp = (warp - 2) >> 2;
         const int q = warp & 3;
         const int r = 32 * q + lane;
         const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
         const uint32_t a_stage = lane_base + (uint32_t)(a_base + 128 * grp);
         uint32_t G[32], M[32];
-        int ri = grp, fi = grp;  // full ring slot of batch t; free ring slot of batch t - 2
+        int ri = grp, fi = grp;  // full slot of this group's next batch; free slot of that batch - 2
         uint32_t fph = 0;
-        for (int t = grp; t < nb; t += kDecodeGroups) {
-            const int pg = t >> 2, sp = pg % kPStages;
-            bool ok = tc::mbar_wait(&pk_full[sp], (pg / kPStages) & 1, err, 31);
-            if (t >= kDecodeGroups) {  // this group's A stage was last read by batch t - 2
-                ok = ok && tc::mbar_wait(&free_[fi], fph, err, 32);
-                fi += kDecodeGroups;
-                if (fi >= R) fi -= R, fph ^= 1;
-            }
-            if (!__all_sync(0xffffffffu, ok)) break;  // TMEM stores below are warp-collective
-            tc::fence_after_sync();
-            const uint8_t *rowp = sP + sp * kPStageBytes + r * 128;
-            const int j0 = (2 * t) & 7;
+        int gb = 0, pgl = 0;     // global batch and packed-stage load index at the item's start
+        bool ok = true;
+        for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
+            const int nb = work_item(args, it).nb;
+            const int nst = (nb + 3) >> 2;
+            for (int pgi = 0; ok && pgi < nst; ++pgi) {
+                const int pg = pgl + pgi, sp = pg % kPStages;
+                ok = __all_sync(0xffffffffu, tc::mbar_wait(&pk_full[sp], (pg / kPStages) & 1, err, 31));
+                if (!ok) break;
+                const int t_end = min(4 * pgi + 4, nb);
+                for (int t = 4 * pgi + (((gb + 4 * pgi) & 1) != grp ? 1 : 0); t < t_end; t += 2) {
+                    if (gb + t >= 2) {  // this group's A stage was last read by global batch gb + t - 2
+                        ok = __all_sync(0xffffffffu, tc::mbar_wait(&free_[fi], fph, err, 32));
+                        fi += 2;
+                        if (fi >= R) fi -= R, fph ^= 1;
+                        if (!ok) break;
+                    }
+                    tc::fence_after_sync();
+                    const uint8_t *rowp = sP + sp * kPStageBytes + r * 128;
+                    const int j0 = (2 * t) & 7;
 #pragma unroll
-            for (int kk = 0; kk < 2; ++kk) {
-                const uint4 v = *reinterpret_cast<const uint4 *>(rowp + (((j0 + kk) ^ (r & 7)) << 4));
-                decode64(v, G, M);
-                tc::tmem_st_x32(a_stage + 32 * kk, G);
-                tc::tmem_st_x32(a_stage + 64 + 32 * kk, M);
+                    for (int kk = 0; kk < 2; ++kk) {
+                        const uint4 v = *reinterpret_cast<const uint4 *>(rowp + (((j0 + kk) ^ (r & 7)) << 4));
+                        decode64(v, G, M);
+                        tc::tmem_st_x32(a_stage + 32 * kk, G);
+                        tc::tmem_st_x32(a_stage + 64 + 32 * kk, M);
+                    }
+                    tc::tmem_wait_st();
+                    tc::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&full[ri]);
+                    ri += 2;
+                    if (ri >= R) ri -= R;
+                }
+                if (!ok) break;
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&pk_empty[sp]);  // done reading this packed stage
             }
-            tc::tmem_wait_st();
-            tc::fence_before_sync();
-            __syncwarp();
-            if (lane == 0) {
-                tc::mbar_arrive(&full[ri]);
-                // last batch of this group inside the packed stage: release the stage
-                if (t + kDecodeGroups > min(4 * pg + 3, nb - 1)) tc::mbar_arrive(&pk_empty[sp]);
-            }
-            ri += kDecodeGroups;
-            if (ri >= R) ri -= R;
+            gb += nb;
+            pgl += nst;
         }
     } else if (warp < kIssuerWarpM) {
         // ---------------------------------------------------------- drain (warps 10..13)
         const int q = warp & 3;
         const int r = 32 * q + lane;
         const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
-        const int row = tile * 128 + r;
         const int k = args.k;
-        double b = 0.0, a = 0.0;
-        if (MODE == kXW && row < args.rows) {
-            b = args.coef[2 * (size_t)row];
-            a = args.coef[2 * (size_t)row + 1];
-        }
-        for (int c = 0; c < kParts * kp; ++c) acc[c * 128 + r] = 0;
-        const int nG = chunk_count(nb, kChunkG, kChunkG), nM = chunk_count(nb, kFirstChunkM, kChunkM);
-        int cG = 0, cM = 0;
+        int cgG = 0, cgM = 0;  // chunks of each accumulator drained so far (all items): barrier parity
         bool ok = true;
-        // drains in the order the chunks end (G' first on a tie)
-        while (ok && (cG < nG || cM < nM)) {
-            const bool g_next = cG < nG && (cM >= nM || chunk_end(cG, nb, kChunkG, kChunkG) <=
-                                                            chunk_end(cM, nb, kFirstChunkM, kChunkM));
-            const int v = g_next ? 0 : 1;
-            const int c = g_next ? cG++ : cM++;
-            ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[v], c & 1, err, 41, true));
-            if (!ok) break;
-            tc::fence_after_sync();
-            // copy the accumulator out (h slices, then l slices), then release it at once
-            const uint32_t cb = lane_base + (uint32_t)(v * N);
-            uint32_t hv[kMaxMixedNrhs], lv[kMaxMixedNrhs];
-#pragma unroll
-            for (int j = 0; j < kMaxMixedNrhs / 8; ++j)
-                if (8 * j < kp) {
-                    tc::tmem_ld_x8(cb + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(hv + 8 * j));
-                    tc::tmem_ld_x8(cb + kp + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(lv + 8 * j));
-                }
-            tc::tmem_wait_ld();
-            tc::fence_before_sync();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&acc_empty[v]);
-            long long *dst = acc + (MODE == kXW ? v * kp * 128 : 0) + r;
-#pragma unroll
-            for (int j = 0; j < kMaxMixedNrhs; ++j)
-                if (j < kp) dst[j * 128] += slices_int(hv[j], lv[j]);
-        }
-        const bool valid = ok && row < args.rows;
-        const double *sc = args.scales + (size_t)win * 4 * k;
-        unsigned int *colmax = args.colmax ? args.colmax + (size_t)win * k : nullptr;
-        const long long *colsumq = args.colsumq ? args.colsumq + (size_t)win * k : nullptr;
-        if (MODE == kXW) {
-            for (int c = 0; c < k; ++c) {
-                float mag = 0.f;
-                if (valid) {
-                    // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum term
-                    const double y = ((b - a) * (double)acc[c * 128 + r] +
-                                      a * (double)(acc[(kp + c) * 128 + r] + colsumq[c])) *
-                                     sc[k + c];
-                    if (args.y_out) args.y_out[(size_t)row * k + c] = y;
-                    args.yt[(int64_t)c * args.yt_ld + row] = (float)y;
-                    mag = (float)(fmax(fabs(b - a), fabs(a)) * fabs(y));
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
-                if (lane == 0 && mag > 0.f) atomicMax(colmax + c, __float_as_uint(mag));
+        for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
+            const WorkItem x = work_item(args, it);
+            const int nb = x.nb;
+            if (nb == 0) continue;
+            const int row = x.tile * 128 + r;
+            double b = 0.0, a = 0.0;
+            if (MODE == kXW && row < args.rows) {
+                b = args.coef[2 * (size_t)row];
+                a = args.coef[2 * (size_t)row + 1];
             }
-        } else if (valid) {
-            double *out = args.partial + ((size_t)split * args.rows + row) * k;
-            for (int c = 0; c < k; ++c) out[c] = (double)acc[c * 128 + r] * sc[3 * k + c];
+            for (int c = 0; c < kParts * kp; ++c) acc[c * 128 + r] = 0;
+            const int nG = chunk_count(nb, kChunkG, kChunkG), nM = chunk_count(nb, kFirstChunkM, kChunkM);
+            int cG = 0, cM = 0;
+            // drains in the order the chunks end (G' first on a tie)
+            while (ok && (cG < nG || cM < nM)) {
+                const bool g_next = cG < nG && (cM >= nM || chunk_end(cG, nb, kChunkG, kChunkG) <=
+                                                                chunk_end(cM, nb, kFirstChunkM, kChunkM));
+                const int v = g_next ? 0 : 1;
+                if (g_next) ++cG;
+                else ++cM;
+                const int cglob = g_next ? cgG++ : cgM++;
+                ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[v], cglob & 1, err, 41, true));
+                if (!ok) break;
+                tc::fence_after_sync();
+                // copy the accumulator out (h slices, then l slices), then release it at once
+                const uint32_t cb = lane_base + (uint32_t)(v * N);
+                uint32_t hv[kMaxMixedNrhs], lv[kMaxMixedNrhs];
+#pragma unroll
+                for (int j = 0; j < kMaxMixedNrhs / 8; ++j)
+                    if (8 * j < kp) {
+                        tc::tmem_ld_x8(cb + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(hv + 8 * j));
+                        tc::tmem_ld_x8(cb + kp + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(lv + 8 * j));
+                    }
+                tc::tmem_wait_ld();
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&acc_empty[v]);
+                long long *dst = acc + (MODE == kXW ? v * kp * 128 : 0) + r;
+#pragma unroll
+                for (int j = 0; j < kMaxMixedNrhs; ++j)
+                    if (j < kp) dst[j * 128] += slices_int(hv[j], lv[j]);
+            }
+            const bool valid = ok && row < args.rows;
+            const double *sc = args.scales + (size_t)x.win * 4 * k;
+            unsigned int *colmax = args.colmax ? args.colmax + (size_t)x.win * k : nullptr;
+            const long long *colsumq = args.colsumq ? args.colsumq + (size_t)x.win * k : nullptr;
+            if (MODE == kXW) {
+                for (int c = 0; c < k; ++c) {
+                    float mag = 0.f;
+                    if (valid) {
+                        // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum term
+                        const double y = ((b - a) * (double)acc[c * 128 + r] +
+                                          a * (double)(acc[(kp + c) * 128 + r] + colsumq[c])) *
+                                         sc[k + c];
+                        if (args.y_out) args.y_out[(size_t)row * k + c] = y;
+                        args.yt[(int64_t)c * args.yt_ld + row] = (float)y;
+                        mag = (float)(fmax(fabs(b - a), fabs(a)) * fabs(y));
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
+                    if (lane == 0 && mag > 0.f) atomicMax(colmax + c, __float_as_uint(mag));
+                }
+            } else if (valid) {
+                double *out = args.partial + ((size_t)x.split * args.rows + row) * k;
+                for (int c = 0; c < k; ++c) out[c] = (double)acc[c * 128 + r] * sc[3 * k + c];
+            }
         }
     }
     tc::fence_before_sync();
@@ -882,7 +932,8 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     DPCA_CUDA(cudaMemsetAsync(m->rq, 0, (size_t)k * 8, h->stream));
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
-        mixed_gemm_kernel<kXW><<<dim3(ceil_div(rows, 128), 1), kThreads, m->smem1, h->stream>>>(map_a, m->map_om, a);
+        a.tiles = a.items = ceil_div(rows, 128);
+        mixed_gemm_kernel<kXW><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(map_a, m->map_om, a);
         DPCA_CUDA(cudaGetLastError());
     }
     ScopedLaunch t(&h->clock, h->stream, "split_bop");
@@ -918,7 +969,9 @@ static dpca_status xty_rows(Handle *h, const CUtensorMap &map_a, int nsnp, doubl
     a.err = h->dflag;
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xty");
-        mixed_gemm_kernel<kXTY><<<dim3(ceil_div(h->n_ind, 128), splits), kThreads, m->smem2, h->stream>>>(
+        a.tiles = ceil_div(h->n_ind, 128);
+        a.items = a.tiles * splits;
+        mixed_gemm_kernel<kXTY><<<std::min(a.items, h->sm_count), kThreads, m->smem2, h->stream>>>(
             map_a, m->map_bop, a);
         DPCA_CUDA(cudaGetLastError());
     }
@@ -967,7 +1020,8 @@ dpca_status mixed_win_pass(Handle *h, const WinPass &p) {
     a.win_active = p.active;
     {
         ScopedLaunch t(&h->clock, h->stream, "win_mixed_xw");
-        mixed_gemm_kernel<kXW><<<dim3(ceil_div(rows, 128), 1), kThreads, m->smem1, h->stream>>>(m->map_p[0], *p.map_om,
+        a.tiles = a.items = ceil_div(rows, 128);
+        mixed_gemm_kernel<kXW><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(m->map_p[0], *p.map_om,
                                                                                                  a);
         DPCA_CUDA(cudaGetLastError());
     }
@@ -997,7 +1051,9 @@ dpca_status mixed_win_pass(Handle *h, const WinPass &p) {
     b.win_active = p.active;
     {
         ScopedLaunch t(&h->clock, h->stream, "win_mixed_xty");
-        mixed_gemm_kernel<kXTY><<<dim3(ceil_div(n, 128), p.W), kThreads, m->smem2, h->stream>>>(m->map_pt[0],
+        b.tiles = ceil_div(n, 128);
+        b.items = b.tiles * p.W;
+        mixed_gemm_kernel<kXTY><<<std::min(b.items, h->sm_count), kThreads, m->smem2, h->stream>>>(m->map_pt[0],
                                                                                                  m->map_bop, b);
         DPCA_CUDA(cudaGetLastError());
     }
