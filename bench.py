@@ -387,18 +387,21 @@ def e2e_run(a, hv) -> dict:
     om0 = D.start_block(a.n_ind, a.nrhs)
     D.run_packed(hv, a.n_ind, omega0=om0, **kw)  # warm-up (context, allocator)
     link = host_link_gbs(hv)
-    times, passes = [], 0
+    times, passes, parts = [], 0, {}
     for _ in range(a.e2e_steps):
         t0 = time.perf_counter()
         r = D.run_packed(hv, a.n_ind, omega0=om0, **kw)
         times.append(time.perf_counter() - t0)
         passes = r["passes"]
+        parts = {"load_s": r["time_load_matrix"], "products_s": r["time_mm"], "qr_s": r["time_gs"],
+                 "rayleigh_ritz_s": r["time_projected_svd"], "other_s": r["time_other"], "streamed": r["streamed"]}
     t = sum(times) / len(times)
     return {"value": a.n_ind * a.n_snp * passes / t, "unit": UNIT,
             "h2d_bytes_per_step": int(hv.nbytes + a.n_ind * a.nrhs * 8),
             "d2h_bytes_per_step": int(a.n_ind * a.nrhs * 8),
             "call": f"dpca_run_packed, 1 outer iteration = {passes} passes incl. H2D, stats, QR, Rayleigh-Ritz",
             "seconds_per_call": t,
+            "breakdown": parts,
             "host_link_gbs": link,
             "note": "the 12.5 GB host-to-device copy is part of each call; host_link_gbs is a plain pinned copy "
                     "measured just before (the host link is shared on this machine and varies between runs)"}

@@ -123,10 +123,6 @@ struct Handle {
     // synchronises the device under the other jobs' work.  dev_bytes counts what is held.
     bool async_alloc = false;
     size_t dev_bytes = 0;
-    // Most blocks of a cooperative (grid-synchronising) launch, 0 = one per SM.  Handles of the
-    // serving loop get sm_count / slots, so that the cooperative grids of all jobs in flight fit
-    // the GPU together: none can wait on blocks that another job's spinning grid keeps out.
-    int coop_blocks = 0;
 
     KernelClock clock;
 };
@@ -144,7 +140,7 @@ size_t handle_footprint(int n_ind, int n_snp, int nrhs, int precision, int sm_co
 size_t mixed_footprint(int n_ind, int n_snp, int nrhs, int sm_count);
 // Resident handle for the serving loop: stream-ordered allocations on `stream`, pageable result mirror.
 dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device,
-                                  cudaStream_t stream, int coop_blocks);
+                                  cudaStream_t stream);
 
 // Offsets (in doubles) inside Handle::small.
 struct SmallLayout {
@@ -183,6 +179,7 @@ dpca_status launch_qr(Handle *h, double *a);
 dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, double *out);  // k x k = A^T B
 dpca_status launch_eig_desc(Handle *h);                                                   // small.B -> W, w
 dpca_status host_sym_eig_desc(int k, const double *B, double *w, double *W);              // eig_host.cpp
+void host_chol_inv(int k, int n, const double *G, bool shift, double *Rinv);               // eig_host.cpp
 dpca_status launch_apply_w(Handle *h, const double *q, double *out);                      // out = Q W
 dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol, int ii, const double *old,
                                        const double *omega);

@@ -127,6 +127,51 @@ dpca_status host_sym_eig_desc(int k, const double *B, double *w, double *W) {
     return DPCA_OK;
 }
 
+// R^-1 of the Cholesky factor of G (+ shift I), both k x k row-major (upper triangle of R^-1,
+// zeros below): one step of the shifted CholeskyQR3 (k_dense.cu launch_qr).  The shift
+// 11 (n k + k (k + 1)) u trace(G) is applied when `shift` is set or when a plain factorization
+// meets a non-positive pivot; a pivot that still fails is replaced by 1 (a zero or non-finite
+// column stays unnormalised instead of dividing by zero).
+void host_chol_inv(int k, int n, const double *G, bool shift, double *Rinv) {
+    std::vector<double> R((size_t)k * k);
+    double tr = 0.0;
+    for (int i = 0; i < k; ++i) tr += G[(size_t)i * k + i];
+    const double s = 11.0 * ((double)n * k + (double)k * (k + 1)) * std::ldexp(1.0, -53) * tr;
+    for (int attempt = shift ? 1 : 0; attempt < 2; ++attempt) {
+        bool broke = false;
+        for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j) R[(size_t)i * k + j] = G[(size_t)i * k + j] + (attempt == 1 && i == j ? s : 0.0);
+        for (int j = 0; j < k && !broke; ++j) {
+            double d = R[(size_t)j * k + j];
+            if (!(d > 0.0) || !std::isfinite(d)) {
+                if (attempt == 0) {
+                    broke = true;
+                    break;
+                }
+                d = 1.0;
+            }
+            const double r = std::sqrt(d), inv = 1.0 / r;
+            R[(size_t)j * k + j] = r;
+            for (int c = j + 1; c < k; ++c) R[(size_t)j * k + c] *= inv;
+            for (int a = j + 1; a < k; ++a) {
+                const double rja = R[(size_t)j * k + a];
+                for (int c = a; c < k; ++c) R[(size_t)a * k + c] -= rja * R[(size_t)j * k + c];
+            }
+        }
+        if (!broke) break;
+    }
+    // R^-1 by back substitution, column by column
+    for (int i = 0; i < k * k; ++i) Rinv[i] = 0.0;
+    for (int c = 0; c < k; ++c) {
+        Rinv[(size_t)c * k + c] = 1.0 / R[(size_t)c * k + c];
+        for (int i = c - 1; i >= 0; --i) {
+            double sum = 0.0;
+            for (int l = i + 1; l <= c; ++l) sum += R[(size_t)i * k + l] * Rinv[(size_t)l * k + c];
+            Rinv[(size_t)i * k + c] = -sum / R[(size_t)i * k + i];
+        }
+    }
+}
+
 }  // namespace dpca
 
 extern "C" dpca_status dpca_sym_eig(int k, const double *b, double *w, double *W) {

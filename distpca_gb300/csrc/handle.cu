@@ -285,12 +285,11 @@ size_t handle_footprint(int n_ind, int n_snp, int nrhs, int precision, int sm_co
 }
 
 dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device,
-                                  cudaStream_t stream, int coop_blocks) {
+                                  cudaStream_t stream) {
     *out = nullptr;
     dpca_handle *hh = new (std::nothrow) dpca_handle();
     if (!hh) return DPCA_ERR_NOMEM;
     hh->h.async_alloc = true;
-    hh->h.coop_blocks = std::max(1, coop_blocks);
     hh->h.stream = stream;  // set before create_impl so that its allocations are ordered on it
     dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream, 0);
     if (st != DPCA_OK) {

@@ -92,7 +92,7 @@ __device__ void block_atb_upper(const double *__restrict__ a, const double *__re
     __syncthreads();
 }
 
-// Thread 0: R = chol(G [+ shift I]) then R^-1 in place (upper, row-major), as chol_inv_kernel.
+// Thread 0: R = chol(G [+ shift I]) then R^-1 in place (upper, row-major), as host_chol_inv.
 __device__ void chol_inv_serial(const double *G, double *R, int k, int n, bool always_shift, double *sinv) {
     double tr = 0.0;
     for (int i = 0; i < k; ++i) tr += G[i * k + i];

@@ -108,10 +108,7 @@ dpca_status run_job(dpca_server *s, Job *j, cudaStream_t stream) {
     const dpca_job &q = j->spec;
     DPCA_CUDA(cudaSetDevice(s->device));
     dpca_handle *hh = nullptr;
-    int sm = 1;
-    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, s->device);
-    dpca_status st = create_serving_handle(&hh, q.n_ind, q.n_snp, q.cfg.nrhs, q.cfg.precision, s->device, stream,
-                                           std::max(1, sm / s->slots));
+    dpca_status st = create_serving_handle(&hh, q.n_ind, q.n_snp, q.cfg.nrhs, q.cfg.precision, s->device, stream);
     if (st == DPCA_OK) {
         if (q.packed)
             st = dpca_upload(hh, q.packed, q.row_stride);
