@@ -4,9 +4,9 @@
 // miss = 1 for missing entries, and per-SNP b = 1/(sd*sqrt(n_snp)), a = -avg*b, the value
 // standardize() gives (utilities.cpp:294-305) is X = b g' + a (1 - miss).  Written with
 //     f1 = g' - miss  in {0, -1, 1, 2} for codes 00, 01, 10, 11,   f2 = relu(f1) = g',
-// it is X[s,i] = a_s + a_s f1[s,i] + (b_s - a_s) f2[s,i]: one table lookup per pair of codes
-// (f1) and one FP16 max (f2) per pair.  The two products of the pass (methods.cpp:853-854,
-// 862-863) become
+// it is X[s,i] = a_s + a_s f1[s,i] + (b_s - a_s) f2[s,i]: one logic op and two FP16 FMAs per
+// pair of codes give f1 and f2 = relu(f1) (decode64).  The two products of the pass
+// (methods.cpp:853-854, 862-863) become
 //     Y  = X Omega  = diag(a) (F1 Omega + 1 colsum(Omega)^T) + diag(b - a) (F2 Omega)   (gemm<kXW>)
 //     Z  = X^T Y    = F1^T (a.Y) + F2^T ((b - a).Y) + 1 (sum_s a_s Y_s)^T               (gemm<kXTY>)
 // where the rank-one terms are exact integer sums of the same quantised operands.
@@ -38,12 +38,13 @@
 //   warp 0       TMA producer: packed 2-bit tiles [128 rows x 128 B] (4 batches) and one 3-D
 //                box of FP16 slice tiles per batch [2 K-blocks][rows][64 elements], 128-byte
 //                swizzled.
-//   warps 1, 14  TMEM allocation (warp 1) and the two MMA-issuing threads
-//                (tcgen05.mma.kind::f16, A from tensor memory, B from shared memory): warp 1
+//   warps 1, 14  TMEM allocation (warp 1) and the two MMA issuers, one elected lane of each
+//                warp (tcgen05.mma.kind::f16, A from tensor memory, B from shared memory): warp 1
 //                issues the f2 products, warp 14 the f1 products, each into its own accumulator.
 //   warps 2..9   decode, two groups of four warps, each owning one TMEM A stage and taking
 //                alternate batches: one thread per tile row turns 2 x 16 packed bytes into
-//                FP16 pairs with byte-permute table lookups and stores them (tcgen05.st).
+//                FP16 pairs (a mask into the mantissa of FP16 1024, then FP16 FMAs) and stores
+//                them (tcgen05.st).
 //   warps 10..13 drain: accumulator chunks (tcgen05.ld) into exact 64-bit integers; outputs.
 // Barriers per batch: one "full" (TMA bytes + the decode group) and one "free" (both issuers'
 // commits), so each issuer waits once and commits once per batch.  Every wait is bounded
@@ -65,6 +66,7 @@ constexpr int kWarps = 15;
 constexpr int kIssuerWarpM = 14;
 constexpr int kThreads = 32 * kWarps;
 constexpr int kDecodeGroups = 2;         // one TMEM A stage per group
+constexpr int kAStages = 2;              // TMEM A stages (batch parity)
 constexpr int kPStages = 3;
 constexpr int kPStageBytes = 128 * 128;  // 128 rows x 128 B = 512 K-elements = 8 K-blocks = 4 batches
 constexpr int kTmemCols = 512;
@@ -125,35 +127,51 @@ struct MixedState {
 
 // ------------------------------------------------------------------ decode
 // K order inside every 16-element group.  Pair register p of a 32-bit word of 16 codes holds
-// the codes at positions a_p and a_p + 4, a_p = (p & 3) + 8 (p >> 2), so that one shift of the
-// word puts both codes where the byte-permute selector needs them (bits 4-5 and 12-13).  The
-// dense operands are stored in the same order: logical K position L of a group holds element
+// code p in its low half and code p + 8 in its high half (16 bits apart, so one mask picks both).
+// The dense operands are stored in the same order: logical K position L of a group holds element
 // perm16(L) of that group.
-__host__ __device__ __forceinline__ int perm16(int L) { return ((L >> 1) & 3) + 8 * (L >> 3) + 4 * (L & 1); }
+__host__ __device__ __forceinline__ int perm16(int L) { return (L >> 1) + 8 * (L & 1); }
 
-__device__ __forceinline__ uint32_t relu_f16x2(uint32_t x) {
-    uint32_t y;
-    asm("fma.rn.relu.f16x2 %0, %1, %2, %3;" : "=r"(y) : "r"(x), "r"(0x3C003C00u), "r"(0u));
-    return y;
+__device__ __forceinline__ uint32_t fma_f16x2(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
 }
 
-// 16 packed bytes = 64 codes -> FP16 pairs: M[8q + p] holds f1 of the pair (a_p, a_p + 4) of
-// word q, G[8q + p] = relu(f1) = g'.  The selector picks, for the high byte of each half, entry
-// c of a 4-byte table; the low bytes select a zero byte.
-//   f1: 00 -> 0, 01 (missing) -> -1.0 (0xBC00), 10 -> 1.0 (0x3C00), 11 -> 2.0 (0x4000)
+__device__ __forceinline__ uint32_t fma_relu_f16x2(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("fma.rn.relu.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+// 16 packed bytes = 64 codes -> FP16 pairs: M[8q + p] holds f1 of the codes (p, p + 8) of word q,
+// G[8q + p] = relu(f1) = g'.
+//   f1: 00 -> 0, 01 (missing) -> -1, 10 -> 1, 11 -> 2;  t = f1 + 1 = c ^ (~c_hi & 1) in {1, 0, 2, 3}
+// One 3-input logic op turns a word of 16 codes c into 16 fields t.  A field at bit offset o (even,
+// o <= 8) of a 16-bit half, ORed into 0x6400 (FP16 1024, whose ulp is 1), is the FP16 value
+// 1024 + t 2^o; one FP16 FMA by 2^-o, minus (1024 2^-o + 1), gives t - 1 = f1 exactly (every
+// intermediate is a small integer or an exact power-of-two multiple).  Codes 0-4 and 8-12 sit at
+// offsets 0-8 of the word's halves; codes 5-7 and 13-15 at offsets 4-8 of the word shifted by 6.
+// So a pair costs one logic op plus two FP16 FMAs (f1, and relu(f1) for g'): the integer pipe,
+// which the byte-table decode loaded with a shift, a mask and a byte permute per pair, is the
+// busier one beside the tensor core.
 __device__ __forceinline__ void decode64(uint4 v, uint32_t (&G)[32], uint32_t (&M)[32]) {
-    const uint32_t TF1 = 0x403CBC00u;
+    // FP16 pairs {2^-o, 2^-o} and {-(1024 2^-o + 1), same} for o = 0, 2, 4, 6, 8
+    const uint32_t kScale[5] = {0x3C003C00u, 0x34003400u, 0x2C002C00u, 0x24002400u, 0x1C001C00u};
+    const uint32_t kBias[5] = {0xE401E401u, 0xDC04DC04u, 0xD410D410u, 0xCC40CC40u, 0xC500C500u};
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const uint32_t x = w[q];
-        const uint32_t sh[8] = {x << 4, x << 2, x, x >> 2, x >> 12, x >> 14, x >> 16, x >> 18};
+        const uint32_t t = x ^ (~(x >> 1) & 0x55555555u);
+        const uint32_t t6 = t >> 6;
 #pragma unroll
         for (int p = 0; p < 8; ++p) {
-            const uint32_t sel = (sh[p] & 0x3030u) | 0x0404u;
-            const uint32_t f1 = __byte_perm(TF1, 0u, sel);
-            M[q * 8 + p] = f1;
-            G[q * 8 + p] = relu_f16x2(f1);
+            const int o = p < 5 ? 2 * p : 2 * (p - 3);  // field offset inside each half
+            const uint32_t src = p < 5 ? t : t6;
+            const uint32_t h = (src & (0x00030003u << o)) | 0x64006400u;
+            M[q * 8 + p] = fma_f16x2(h, kScale[o >> 1], kBias[o >> 1]);
+            G[q * 8 + p] = fma_relu_f16x2(h, kScale[o >> 1], kBias[o >> 1]);
         }
     }
 }
@@ -306,30 +324,36 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     } else if (warp == 1 || warp == kIssuerWarpM) {
         // ---------------------------------------------------------- MMA issuers
-        if (lane == 0) {
-            const int v = warp == 1 ? 0 : 1;  // 0: G' products, 1: M products
-            const int first_len = v ? kFirstChunkM : kChunkG, len = v ? kChunkM : kChunkG;
-            const uint32_t idesc = tc::idesc_f16_f32(128, N);
-            // B stage r, K-block j, K step s: stage base + j * tile_bytes (+ N rows for the X^T Y
-            // M products) + 32 s bytes; descriptors count 16-byte units
-            const uint64_t bdesc0 =
-                tc::desc_kmajor_sw128(tc::smem_u32(sB) + (MODE == kXTY ? (uint32_t)(v * N * 128) : 0u));
-            const uint64_t tile_units = (uint64_t)(tile_bytes >> 4);
-            const uint32_t d = tbase + (uint32_t)(v * N);
-            const uint32_t a_v = tbase + (uint32_t)(a_base + 64 * v);
-            int r = 0, cv = 0;  // B ring slot; chunks of this accumulator committed (all items)
-            uint32_t ph = 0, stage = 0;  // stage = global batch parity
-            bool ok = true;
-            for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
-                const int nb = work_item(args, it).nb;
-                int left = first_len;
-                bool fresh = true;
-                for (int t = 0; t < nb; ++t) {
-                    if (!(ok = wait_fast(&full[r], ph, err, 21))) break;
-                    if (fresh && cv > 0 && !(ok = wait_fast(&acc_empty[v], (cv - 1) & 1, err, 22))) break;
-                    tc::fence_after_sync();
-                    const uint64_t b1 = bdesc0 + (uint64_t)((r * bstage) >> 4), b2 = b1 + tile_units;
-                    const uint32_t a = a_v + 128u * stage;
+        // The whole warp runs the loop (its waits and ring bookkeeping), so every operand of the
+        // MMAs is warp-uniform; one elected lane issues the MMAs and commits.  Issued from a
+        // single-lane branch instead, each MMA cost ~110 issue cycles against 40 tensor cycles.
+        const int v = warp == 1 ? 0 : 1;  // 0: G' products, 1: M products
+        const int first_len = v ? kFirstChunkM : kChunkG, len = v ? kChunkM : kChunkG;
+        const uint32_t idesc = tc::idesc_f16_f32(128, N);
+        // B stage r, K-block j, K step s: stage base + j * tile_bytes (+ N rows for the X^T Y
+        // M products) + 32 s bytes; descriptors count 16-byte units
+        const uint64_t bdesc0 =
+            tc::desc_kmajor_sw128(tc::smem_u32(sB) + (MODE == kXTY ? (uint32_t)(v * N * 128) : 0u));
+        const uint64_t tile_units = (uint64_t)(tile_bytes >> 4);
+        const uint32_t d = tbase + (uint32_t)(v * N);
+        const uint32_t a_v = tbase + (uint32_t)(a_base + 64 * v);
+        int r = 0, cv = 0;  // B ring slot; chunks of this accumulator committed (all items)
+        uint32_t ph = 0, stage = 0;  // stage = global batch parity
+        bool ok = true;
+        for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
+            const int nb = work_item(args, it).nb;
+            int left = first_len;
+            bool fresh = true;
+            for (int t = 0; t < nb; ++t) {
+                if (!(ok = __all_sync(0xffffffffu, wait_fast(&full[r], ph, err, 21)))) break;
+                if (fresh && cv > 0 &&
+                    !(ok = __all_sync(0xffffffffu, wait_fast(&acc_empty[v], (cv - 1) & 1, err, 22))))
+                    break;
+                const bool chunk_done = --left == 0 || t == nb - 1;
+                tc::fence_after_sync();
+                const uint64_t b1 = bdesc0 + (uint64_t)((r * bstage) >> 4), b2 = b1 + tile_units;
+                const uint32_t a = a_v + 128u * stage;
+                if (tc::elect_one_sync()) {
                     tc::mma_ts_f16(d, a, b1, idesc, fresh ? 0u : 1u);
                     tc::mma_ts_f16(d, a + 8, b1 + 2, idesc, 1u);
                     tc::mma_ts_f16(d, a + 16, b1 + 4, idesc, 1u);
@@ -339,16 +363,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tc::mma_ts_f16(d, a + 48, b2 + 4, idesc, 1u);
                     tc::mma_ts_f16(d, a + 56, b2 + 6, idesc, 1u);
                     tc::mma_commit(&free_[r]);
-                    fresh = false;
-                    if (--left == 0 || t == nb - 1) {
-                        tc::mma_commit(&acc_full[v]);
-                        ++cv;
-                        left = len;
-                        fresh = true;
-                    }
-                    if (++r == R) r = 0, ph ^= 1;
-                    stage ^= 1u;
+                    if (chunk_done) tc::mma_commit(&acc_full[v]);
                 }
+                __syncwarp();
+                fresh = false;
+                if (chunk_done) {
+                    ++cv;
+                    left = len;
+                    fresh = true;
+                }
+                if (++r == R) r = 0, ph ^= 1;
+                stage ^= 1u;
             }
         }
     } else if (warp >= 2 && warp < 2 + 4 * kDecodeGroups) {
@@ -836,7 +861,7 @@ dpca_status mixed_prepare(Handle *h) {
         return DPCA_ERR_UNSUPPORTED;
     }
     const int N = m->N;
-    if (((2 * N + 31) & ~31) + 128 * kDecodeGroups > kTmemCols) {
+    if (((2 * N + 31) & ~31) + 128 * kAStages > kTmemCols) {
         set_error("internal: TMEM budget exceeded for nrhs %d", k);
         return DPCA_ERR_UNSUPPORTED;
     }

@@ -178,6 +178,19 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw128(uint32_t smem_addr) {
     return d;
 }
 
+// True in one lane of the converged warp (the same lane on every call).  Single-thread tcgen05
+// operations (mma, commit) are issued under it while the whole warp runs the loop around them,
+// so the loop's operands stay warp-uniform and reach the tensor core from uniform registers.
+__device__ __forceinline__ bool elect_one_sync() {
+    uint32_t pred = 0;
+    asm volatile(
+        "{\n\t.reg .b32 rx;\n\t.reg .pred px;\n\t"
+        "elect.sync rx|px, 0xffffffff;\n\t"
+        "selp.b32 %0, 1, 0, px;\n\t}"
+        : "+r"(pred));
+    return pred != 0;
+}
+
 // D (tmem) = [D +] A (tmem) x B (smem), M x N x 16.
 __device__ __forceinline__ void mma_ts_f16(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
                                            uint32_t accumulate) {
