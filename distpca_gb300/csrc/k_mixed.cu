@@ -192,6 +192,46 @@ __device__ __forceinline__ long long slices_int(uint32_t hbits, uint32_t lbits) 
            (long long)__float2int_rz(__uint_as_float(lbits));
 }
 
+// Double-float arithmetic: a value hi + lo of two FP32 numbers carries ~48 bits.  The X Omega
+// epilogue combines exact 64-bit integer sums with FP64 per-SNP coefficients; GB300's FP64 pipe
+// runs at a small fraction of its FP32 rate, and ~11 FP64 operations per output element made
+// the epilogue, not the MMAs, the cost of every short-K tile (cohorts of a few thousand).  So the
+// combination is formed from error-free FP32 products (FMA) and compensated sums (Knuth's
+// TwoSum), then rounded once to FP32.  The _rn intrinsics keep the compiler from contracting them.
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+// FP64 coefficient -> hi + lo
+__device__ __forceinline__ DF df_from_double(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
+// A power of two held in FP64 (|exponent| < 127) as FP32, by integer arithmetic on its exponent.
+__device__ __forceinline__ float pow2_to_float(double x) {
+    const long long bits = __double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7FF) - 1023;
+    return __int_as_float((int)(bits >> 32 & 0x80000000) | ((e + 127) << 23));
+}
+
+// c * x for an exact integer x (|x| < 2^48: x = H 2^24 + L with H, L exact in FP32).
+__device__ __forceinline__ DF df_mul_int(DF c, long long x) {
+    const float xh = __fmul_rn((float)(int)(x >> 24), 16777216.f);
+    const float xl = (float)(int)(x & 0xFFFFFF);
+    const float p1 = __fmul_rn(c.hi, xh), p2 = __fmul_rn(c.hi, xl);
+    const float e1 = __fmaf_rn(c.hi, xh, -p1), e2 = __fmaf_rn(c.hi, xl, -p2);
+    const DF s = df_two_sum(p1, p2);
+    const float t = __fmaf_rn(c.lo, __fadd_rn(xh, xl), __fadd_rn(__fadd_rn(e1, e2), s.lo));
+    return df_two_sum(s.hi, t);
+}
+
 // Slow path of a wait, out of line so that the MMA issue loop stays compact (an inlined wait
 // loop in that loop costs ~90 cycles per iteration even when it never runs).
 __device__ __noinline__ bool wait_slow(uint64_t *bar, uint32_t parity, int *err, int code) {
@@ -251,6 +291,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t *full = pk_empty + kPStages, *free_ = full + R;
     uint64_t *acc_full = free_ + R, *acc_empty = acc_full + 2;
     uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
+    // X Omega column maxima of this CTA's tiles (one global atomic per column per CTA at the end;
+    // per-warp global atomics on the same k addresses from every CTA stalled short-K tiles)
+    unsigned int *cmax_s = tmem_slot + 1;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *err = args.err;
@@ -269,6 +312,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc::mbar_init(&acc_empty[v], 4);
         }
         tc::fence_mbar_init();
+        for (int c = 0; c < kMaxMixedNrhs; ++c) cmax_s[c] = 0u;
         tc::tma_prefetch(&map_a);
         tc::tma_prefetch(&map_b);
     }
@@ -448,6 +492,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 b = args.coef[2 * (size_t)row];
                 a = args.coef[2 * (size_t)row + 1];
             }
+            const DF cba = df_from_double(b - a), ca = df_from_double(a);
+            const float cmax = (float)fmax(fabs(b - a), fabs(a));
             for (int c = 0; c < kParts * kp; ++c) acc[c * 128 + r] = 0;
             const int nG = chunk_count(nb, kChunkG, kChunkG), nM = chunk_count(nb, kFirstChunkM, kChunkM);
             int cG = 0, cM = 0;
@@ -484,31 +530,53 @@ __global__ void __launch_bounds__(kThreads, 1)
             const double *sc = args.scales + (size_t)x.win * 4 * k;
             unsigned int *colmax = args.colmax ? args.colmax + (size_t)x.win * k : nullptr;
             const long long *colsumq = args.colsumq ? args.colsumq + (size_t)x.win * k : nullptr;
+            // Per-column values of this item: lane l holds columns l and l + 32 (k <= 48), loaded
+            // together and broadcast by shuffles in the column loop.  Loaded inside the loop, each
+            // column waited a global-memory round trip behind the previous column's stores, which
+            // made the epilogue the cost of short-K tiles.
+            const int c0 = lane, c1 = lane + 32;
             if (MODE == kXW) {
+                const float inv0 = c0 < k ? pow2_to_float(sc[k + c0]) : 0.f;
+                const float inv1 = c1 < k ? pow2_to_float(sc[k + c1]) : 0.f;
+                const long long cs0 = c0 < k ? colsumq[c0] : 0, cs1 = c1 < k ? colsumq[c1] : 0;
                 for (int c = 0; c < k; ++c) {
+                    const float inv = __shfl_sync(0xffffffffu, c < 32 ? inv0 : inv1, c & 31);
+                    const long long cs = __shfl_sync(0xffffffffu, c < 32 ? cs0 : cs1, c & 31);
                     float mag = 0.f;
                     if (valid) {
-                        // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum term
-                        const double y = ((b - a) * (double)acc[c * 128 + r] +
-                                          a * (double)(acc[(kp + c) * 128 + r] + colsumq[c])) *
-                                         sc[k + c];
-                        if (args.y_out) args.y_out[(size_t)row * k + c] = y;
-                        args.yt[(int64_t)c * args.yt_ld + row] = (float)y;
-                        mag = (float)(fmax(fabs(b - a), fabs(a)) * fabs(y));
+                        // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum term.
+                        // y = ((b - a) A2 + a A1) / scale_c, the scale a power of two (exact).
+                        const DF u = df_mul_int(cba, acc[c * 128 + r]);
+                        const DF v = df_mul_int(ca, acc[(kp + c) * 128 + r] + cs);
+                        const DF t = df_two_sum(u.hi, v.hi);
+                        const DF y = df_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(u.lo, v.lo)));
+                        const float yf = __fmul_rn(y.hi, inv);
+                        if (args.y_out) args.y_out[(size_t)row * k + c] = ((double)y.hi + (double)y.lo) * (double)inv;
+                        args.yt[(int64_t)c * args.yt_ld + row] = yf;
+                        mag = cmax * fabsf(yf);
                     }
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
-                    if (lane == 0 && mag > 0.f) atomicMax(colmax + c, __float_as_uint(mag));
+                    if (lane == 0 && mag > 0.f) {
+                        if (args.tile_win) atomicMax(colmax + c, __float_as_uint(mag));  // per window
+                        else atomicMax(cmax_s + c, __float_as_uint(mag));
+                    }
                 }
-            } else if (valid) {
-                double *out = args.partial + ((size_t)x.split * args.rows + row) * k;
-                for (int c = 0; c < k; ++c) out[c] = (double)acc[c * 128 + r] * sc[3 * k + c];
+            } else {
+                const double s0 = c0 < k ? sc[3 * k + c0] : 0.0, s1 = c1 < k ? sc[3 * k + c1] : 0.0;
+                double *out = args.partial + ((size_t)x.split * args.rows + (valid ? row : 0)) * k;
+                for (int c = 0; c < k; ++c) {
+                    const double scl = __shfl_sync(0xffffffffu, c < 32 ? s0 : s1, c & 31);
+                    if (valid) out[c] = (double)acc[c * 128 + r] * scl;
+                }
             }
         }
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    if (MODE == kXW && !args.tile_win && threadIdx.x < args.k && cmax_s[threadIdx.x] != 0u)
+        atomicMax(args.colmax + threadIdx.x, cmax_s[threadIdx.x]);
     if (warp == 1) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
