@@ -539,27 +539,41 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const float inv0 = c0 < k ? pow2_to_float(sc[k + c0]) : 0.f;
                 const float inv1 = c1 < k ? pow2_to_float(sc[k + c1]) : 0.f;
                 const long long cs0 = c0 < k ? colsumq[c0] : 0, cs1 = c1 < k ? colsumq[c1] : 0;
-                for (int c = 0; c < k; ++c) {
-                    const float inv = __shfl_sync(0xffffffffu, c < 32 ? inv0 : inv1, c & 31);
-                    const long long cs = __shfl_sync(0xffffffffu, c < 32 ? cs0 : cs1, c & 31);
-                    float mag = 0.f;
-                    if (valid) {
-                        // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum term.
-                        // y = ((b - a) A2 + a A1) / scale_c, the scale a power of two (exact).
-                        const DF u = df_mul_int(cba, acc[c * 128 + r]);
-                        const DF v = df_mul_int(ca, acc[(kp + c) * 128 + r] + cs);
-                        const DF t = df_two_sum(u.hi, v.hi);
-                        const DF y = df_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(u.lo, v.lo)));
-                        const float yf = __fmul_rn(y.hi, inv);
-                        if (args.y_out) args.y_out[(size_t)row * k + c] = ((double)y.hi + (double)y.lo) * (double)inv;
-                        args.yt[(int64_t)c * args.yt_ld + row] = yf;
-                        mag = cmax * fabsf(yf);
+                // two columns at a time: their dependent FP32 chains interleave (one drain warp per
+                // SM sub-partition runs this loop, so it is latency-bound one column at a time)
+                for (int c = 0; c < k; c += 2) {
+                    float mg[2];
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const int cc = c + j;  // < 50: lanes past k hold zeros
+                        const float inv = __shfl_sync(0xffffffffu, cc < 32 ? inv0 : inv1, cc & 31);
+                        const long long cs = __shfl_sync(0xffffffffu, cc < 32 ? cs0 : cs1, cc & 31);
+                        mg[j] = 0.f;
+                        if (valid && cc < k) {
+                            // acc part 0: f2 products, part 1: f1 products; plus the rank-one colsum
+                            // term.  y = ((b - a) A2 + a A1) / scale_c, the scale a power of two (exact).
+                            const DF u = df_mul_int(cba, acc[cc * 128 + r]);
+                            const DF v = df_mul_int(ca, acc[(kp + cc) * 128 + r] + cs);
+                            const DF t = df_two_sum(u.hi, v.hi);
+                            const DF y = df_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(u.lo, v.lo)));
+                            const float yf = __fmul_rn(y.hi, inv);
+                            if (args.y_out) args.y_out[(size_t)row * k + cc] = ((double)y.hi + (double)y.lo) * (double)inv;
+                            args.yt[(int64_t)cc * args.yt_ld + row] = yf;
+                            mg[j] = cmax * fabsf(yf);
+                        }
                     }
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, o));
-                    if (lane == 0 && mag > 0.f) {
-                        if (args.tile_win) atomicMax(colmax + c, __float_as_uint(mag));  // per window
-                        else atomicMax(cmax_s + c, __float_as_uint(mag));
+                    for (int o = 16; o > 0; o >>= 1) {
+                        mg[0] = fmaxf(mg[0], __shfl_xor_sync(0xffffffffu, mg[0], o));
+                        mg[1] = fmaxf(mg[1], __shfl_xor_sync(0xffffffffu, mg[1], o));
+                    }
+                    if (lane == 0) {
+#pragma unroll
+                        for (int j = 0; j < 2; ++j)
+                            if (c + j < k && mg[j] > 0.f) {
+                                if (args.tile_win) atomicMax(colmax + c + j, __float_as_uint(mg[j]));  // per window
+                                else atomicMax(cmax_s + c + j, __float_as_uint(mg[j]));
+                            }
                     }
                 }
             } else {
