@@ -56,11 +56,20 @@ __global__ void __launch_bounds__(256) atb_kernel(const double *__restrict__ A, 
     }
 }
 
-__global__ void sum_parts_kernel(const double *__restrict__ part, int nparts, int elems, double *__restrict__ out) {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < elems; e += gridDim.x * blockDim.x) {
+// out[e] = sum over p of part[p][e]: one warp per element, its lanes taking every 32nd part, then
+// a fixed-order shuffle reduction (deterministic).  With one thread per element the k^2 sums ran
+// on k^2 / 256 blocks, each thread walking all parts: ~36 us per Gram at 12,919 x 40, more than
+// the Gram itself.
+__global__ void __launch_bounds__(256) sum_parts_kernel(const double *__restrict__ part, int nparts, int elems,
+                                                        double *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < elems; e += warps) {
         double s = 0.0;
-        for (int p = 0; p < nparts; ++p) s += part[(size_t)p * elems + e];
-        out[e] = s;
+        for (int p = lane; p < nparts; p += 32) s += part[(size_t)p * elems + e];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) out[e] = s;
     }
 }
 
@@ -84,7 +93,8 @@ static dpca_status atb_timed(Handle *h, const double *a, const double *b, int n,
     }
     {
         ScopedLaunch t(&h->clock, h->stream, sum_name);
-        sum_parts_kernel<<<ceil_div(kk, 256), 256, 0, h->stream>>>(h->red, nparts, kk, out);
+        sum_parts_kernel<<<std::min(ceil_div(kk * 32, 256), 8 * h->sm_count), 256, 0, h->stream>>>(h->red, nparts, kk,
+                                                                                                 out);
         DPCA_CUDA(cudaGetLastError());
     }
     return DPCA_OK;

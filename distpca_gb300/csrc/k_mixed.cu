@@ -214,10 +214,14 @@ __device__ __forceinline__ DF df_from_double(double x) {
     return {h, (float)(x - (double)h)};
 }
 
-// A power of two held in FP64 (|exponent| < 127) as FP32, by integer arithmetic on its exponent.
+// A power of two held in FP64 as FP32, by integer arithmetic on its exponent; 0 when it is not an
+// FP32 normal number (an Omega column below ~1e-31 or above ~1e45), for which the caller falls back
+// to FP64.  (Y itself is FP32, so the mixed pass serves Omega columns of about 1e-30 to 1e37; the
+// solver's Omega is orthonormal.)
 __device__ __forceinline__ float pow2_to_float(double x) {
     const long long bits = __double_as_longlong(x);
     const int e = (int)((bits >> 52) & 0x7FF) - 1023;
+    if (e < -126 || e > 127) return 0.f;
     return __int_as_float((int)(bits >> 32 & 0x80000000) | ((e + 127) << 23));
 }
 
@@ -556,8 +560,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                             const DF v = df_mul_int(ca, acc[(kp + cc) * 128 + r] + cs);
                             const DF t = df_two_sum(u.hi, v.hi);
                             const DF y = df_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(u.lo, v.lo)));
-                            const float yf = __fmul_rn(y.hi, inv);
-                            if (args.y_out) args.y_out[(size_t)row * k + cc] = ((double)y.hi + (double)y.lo) * (double)inv;
+                            float yf;
+                            double yd = 0.0;
+                            if (inv != 0.f) {  // uniform per column
+                                yf = __fmul_rn(y.hi, inv);
+                                if (args.y_out) yd = ((double)y.hi + (double)y.lo) * (double)inv;
+                            } else {  // scale outside the FP32 normal range: FP64
+                                yd = ((double)y.hi + (double)y.lo) * sc[k + cc];
+                                yf = (float)yd;
+                            }
+                            if (args.y_out) args.y_out[(size_t)row * k + cc] = yd;
                             args.yt[(int64_t)cc * args.yt_ld + row] = yf;
                             mg[j] = cmax * fabsf(yf);
                         }

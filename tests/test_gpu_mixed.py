@@ -59,6 +59,26 @@ def test_pass_ragged_shapes_vs_fp64(dpca, n_ind, n_snp, k):
     assert rel_max(z, zf) < 3e-6
 
 
+def test_pass_columns_of_far_apart_magnitudes(dpca):
+    """Each Omega column gets its own power-of-two fixed-point scale, and the X Omega epilogue
+    removes it by exponent arithmetic: columns from 1e-20 to 1e20 must each match the FP64 pass
+    to the per-column tolerance."""
+    from distpca_gb300 import synth
+
+    n_ind, n_snp, k = 700, 3000, 6
+    c = synth.make_cohort(n_ind, n_snp, n_pop=3, fst=0.05, missing=0.02, seed=11)
+    packed = synth.pack_rows(c)
+    om = np.random.default_rng(3).standard_normal((n_ind, k)) * np.array([1e-20, 1e-9, 1.0, 3e5, 1e12, 1e20])
+    with dpca.Handle(n_ind, n_snp, k, precision="fp64") as h:
+        h.upload(packed)
+        h.set_omega(om)
+        h.pass_()
+        zf = h.z()
+    z = mixed_z(dpca, packed, n_ind, om)
+    for j in range(k):
+        assert rel_max(z[:, j], zf[:, j]) < 3e-6, j
+
+
 def test_pass_deterministic(dpca):
     prefix, n_ind, n_snp, packed = fileset("wide")
     om = dpca.start_block(n_ind, 20)
