@@ -34,7 +34,9 @@
 // instruction it issues, against 40 tensor-core cycles per M=128, N=80, K=16 MMA, so a wait and
 // a commit must be spread over at least eight MMAs per issuer to keep the tensor core busy.
 //
-// CTA structure (one CTA per 128-row output tile and K split, 480 threads, 1 CTA per SM):
+// Work items are (128-row output tile, K split) pairs.  X Omega, and X^T Y with short items, run
+// one persistent CTA per SM walking items blockIdx.x, blockIdx.x + gridDim.x, ...; long X^T Y
+// items get one CTA each.  CTA structure (480 threads, 1 CTA per SM: it owns all of TMEM):
 //   warp 0       TMA producer: packed 2-bit tiles [128 rows x 128 B] (4 batches) and one 3-D
 //                box of FP16 slice tiles per batch [2 K-blocks][rows][64 elements], 128-byte
 //                swizzled.
@@ -45,7 +47,8 @@
 //                alternate batches: one thread per tile row turns 2 x 16 packed bytes into
 //                FP16 pairs (a mask into the mantissa of FP16 1024, then FP16 FMAs) and stores
 //                them (tcgen05.st).
-//   warps 10..13 drain: accumulator chunks (tcgen05.ld) into exact 64-bit integers; outputs.
+//   warps 10..13 drain: accumulator chunks (tcgen05.ld) into exact 64-bit integers; the tile's
+//                outputs (X Omega: Y in FP32 and column maxima; X^T Y: FP64 K-split partials).
 // Barriers per batch: one "full" (TMA bytes + the decode group) and one "free" (both issuers'
 // commits), so each issuer waits once and commits once per batch.  Every wait is bounded
 // (tc.cuh) and reports through h->dflag.
