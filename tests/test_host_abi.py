@@ -236,6 +236,30 @@ def test_sym_eig_matches_numpy(dpca, k):
         assert np.abs(a @ W - W * w).max() <= 1e-12 * scale
 
 
+@pytest.mark.parametrize("n_ind,n_snp,nrhs,prec,status", [
+    (0, 100, 4, "fp64", 1),       # no individuals
+    (100, 0, 4, "mixed", 1),      # no SNPs
+    (100, 100, 0, "mixed", 1),    # no right-hand sides
+    (-5, 100, 4, "fp64", 1),
+    (100, 100, 129, "fp64", 6),   # beyond the kernels' nrhs limit
+    (100, 100, 4, 7, 1),          # unknown precision
+])
+def test_empty_and_oversized_shapes_rejected_before_the_device(dpca, n_ind, n_snp, nrhs, prec, status):
+    # dpca_create (and its streamed form) validate the shape before any CUDA call, so these
+    # status codes are the same with or without a GPU
+    for block_snps in (0, 64):
+        with pytest.raises(dpca.DpcaError) as e:
+            dpca.Handle(n_ind, n_snp, nrhs, precision=prec, block_snps=block_snps)
+        assert e.value.status == status, (block_snps, e.value.message)
+
+
+def test_start_block_rejects_empty_shapes(dpca):
+    for n, k in ((0, 4), (10, 0)):
+        with pytest.raises(dpca.DpcaError) as e:
+            dpca.start_block(n, k)
+        assert e.value.status == 1
+
+
 def test_windows_reject_bad_shapes_before_the_device(dpca):
     # checked before any device work, so these hold without a GPU too
     with pytest.raises(dpca.DpcaError) as e:
