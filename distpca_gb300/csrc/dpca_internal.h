@@ -122,25 +122,30 @@ struct Handle {
     // for handles of the serving loop, so that creating and freeing one job's buffers never
     // synchronises the device under the other jobs' work.  dev_bytes counts what is held.
     bool async_alloc = false;
+    cudaMemPool_t pool = nullptr;  // the pool stream-ordered allocations come from (NULL: the device's default)
     size_t dev_bytes = 0;
 
     KernelClock clock;
 };
 
 // Raise a kernel's dynamic shared-memory limit to the current device's opt-in maximum, once
-// per (kernel, device).  The limit is a process-wide function attribute: setting it to each
+// per (kernel, CUDA context).  The limit is a process-wide function attribute: setting it to each
 // launch's own size races between host threads that launch the same kernel with different
-// sizes (the serving loop's workers), so it is set once, to the largest value.
+// sizes (the serving loop's workers), so it is set once, to the largest value.  It belongs to
+// the context, so a context created later (after cudaDeviceReset) gets it set again.
 dpca_status allow_max_smem(const void *func);
+// Unique id (cuCtxGetId) of the calling thread's current CUDA context.
+dpca_status current_context_id(unsigned long long *id);
 
 dpca_status dev_alloc(Handle *h, void **p, size_t bytes);
 void dev_free(Handle *h, void *p);
 // Device bytes a resident handle of these sizes holds (what create_impl and mixed_prepare allocate).
 size_t handle_footprint(int n_ind, int n_snp, int nrhs, int precision, int sm_count);
 size_t mixed_footprint(int n_ind, int n_snp, int nrhs, int sm_count);
-// Resident handle for the serving loop: stream-ordered allocations on `stream`, pageable result mirror.
+// Resident handle for the serving loop: stream-ordered allocations from `pool` on `stream`, pageable
+// result mirror.
 dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device,
-                                  cudaStream_t stream);
+                                  cudaStream_t stream, cudaMemPool_t pool);
 
 // Offsets (in doubles) inside Handle::small.
 struct SmallLayout {

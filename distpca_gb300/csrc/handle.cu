@@ -85,27 +85,73 @@ bool env_flag(const char *name) {
 
 static size_t round_up(size_t a, size_t b) { return (a + b - 1) / b * b; }
 
+// The driver's unique id of the calling thread's current context (cuCtxGetId), made current by
+// a runtime call first.  Unlike a device ordinal or a CUcontext handle, the id of a context
+// created after cudaDeviceReset (or a different context the caller made current) differs from
+// the old one's, so state cached per context -- kernel attributes, symbol addresses -- is
+// looked up again instead of being reused from a context that no longer exists.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+dpca_status current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (CtxGetCurrentFn)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (CtxGetIdFn)p;
+    });
+    if (!get_current || !get_id) {
+        set_error("the CUDA driver does not provide cuCtxGetCurrent/cuCtxGetId");
+        return DPCA_ERR_CUDA;
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) == CUDA_SUCCESS && !ctx) {
+        // no context yet on this thread: cudaSetDevice makes the device's primary context current
+        int dev = 0;
+        DPCA_CUDA(cudaGetDevice(&dev));
+        DPCA_CUDA(cudaSetDevice(dev));
+        get_current(&ctx);
+    }
+    if (!ctx || get_id(ctx, id) != CUDA_SUCCESS) {
+        set_error("no current CUDA context");
+        return DPCA_ERR_CUDA;
+    }
+    return DPCA_OK;
+}
+
 dpca_status allow_max_smem(const void *func) {
     static std::mutex mu;
-    static std::set<std::pair<const void *, int>> done;
+    static std::set<std::pair<const void *, unsigned long long>> done;
     int dev = 0;
     DPCA_CUDA(cudaGetDevice(&dev));
+    unsigned long long ctx = 0;
+    DPCA_TRY(current_context_id(&ctx));
     std::lock_guard<std::mutex> lk(mu);
-    if (done.count({func, dev})) return DPCA_OK;
+    if (done.count({func, ctx})) return DPCA_OK;
     int optin = 0;
     DPCA_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fa{};
     DPCA_CUDA(cudaFuncGetAttributes(&fa, func));
     DPCA_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    optin - (int)fa.sharedSizeBytes));
-    done.insert({func, dev});
+    done.insert({func, ctx});
     return DPCA_OK;
 }
 
 dpca_status dev_alloc(Handle *h, void **p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) return DPCA_OK;
-    cudaError_t e = h->async_alloc ? cudaMallocAsync(p, bytes, h->stream) : cudaMalloc(p, bytes);
+    cudaError_t e = !h->async_alloc ? cudaMalloc(p, bytes)
+                    : h->pool       ? cudaMallocFromPoolAsync(p, bytes, h->pool, h->stream)
+                                    : cudaMallocAsync(p, bytes, h->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         set_error("device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
@@ -285,11 +331,12 @@ size_t handle_footprint(int n_ind, int n_snp, int nrhs, int precision, int sm_co
 }
 
 dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int nrhs, int precision, int device,
-                                  cudaStream_t stream) {
+                                  cudaStream_t stream, cudaMemPool_t pool) {
     *out = nullptr;
     dpca_handle *hh = new (std::nothrow) dpca_handle();
     if (!hh) return DPCA_ERR_NOMEM;
     hh->h.async_alloc = true;
+    hh->h.pool = pool;
     hh->h.stream = stream;  // set before create_impl so that its allocations are ordered on it
     dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream, 0);
     if (st != DPCA_OK) {
@@ -827,8 +874,11 @@ dpca_status dpca_reset_kernel_times(dpca_handle *hh, int enable) {
 dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp, int32_t *counts,
                                double *avg, double *sd) {
     clear_error();
+    // on the calling thread's current device (cudaSetDevice before the call picks another)
+    int dev = 0;
+    DPCA_CUDA(cudaGetDevice(&dev));
     dpca_handle *hh = nullptr;
-    DPCA_TRY(dpca_create(&hh, n_ind, n_snp, 1, DPCA_PREC_FP64, 0, nullptr));
+    DPCA_TRY(dpca_create(&hh, n_ind, n_snp, 1, DPCA_PREC_FP64, dev, nullptr));
     dpca_status st = dpca_upload(hh, packed, row_stride);
     if (st == DPCA_OK) st = dpca_snp_stats(hh, counts, avg, sd, nullptr);
     dpca_destroy(hh);

@@ -139,21 +139,22 @@ __global__ void reduce_splits_kernel(const double *__restrict__ partial, int64_t
 }
 
 template <int MAXC>
-static void xw_launch(Handle *h, const double *omega, double *y) {
+static dpca_status xw_launch(Handle *h, const double *omega, double *y) {
     size_t smem = (size_t)64 * h->k * sizeof(double);
     // opt in above the default 48 KB (static shared memory counts against it as well)
-    allow_max_smem((const void *)fp64_xw_kernel<MAXC>);
+    DPCA_TRY(allow_max_smem((const void *)fp64_xw_kernel<MAXC>));
     fp64_xw_kernel<MAXC><<<ceil_div(h->n_snp, 64), 256, smem, h->stream>>>(h->P, h->pitch, h->lut, h->n_ind,
                                                                             h->n_snp, h->k, omega, y);
+    return DPCA_OK;
 }
 
 dpca_status launch_fp64_xw(Handle *h, const double *omega, double *y) {
     ScopedLaunch t(&h->clock, h->stream, "fp64_xw");
     int mc = (h->k + 3) / 4;
-    if (mc <= 4) xw_launch<4>(h, omega, y);
-    else if (mc <= 8) xw_launch<8>(h, omega, y);
-    else if (mc <= 16) xw_launch<16>(h, omega, y);
-    else xw_launch<32>(h, omega, y);
+    if (mc <= 4) DPCA_TRY(xw_launch<4>(h, omega, y));
+    else if (mc <= 8) DPCA_TRY(xw_launch<8>(h, omega, y));
+    else if (mc <= 16) DPCA_TRY(xw_launch<16>(h, omega, y));
+    else DPCA_TRY(xw_launch<32>(h, omega, y));
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -169,12 +170,13 @@ static int xty_splits(const Handle *h) {
 }
 
 template <int MAXC>
-static void xty_launch(Handle *h, const double *y, int splits, int sps) {
+static dpca_status xty_launch(Handle *h, const double *y, int splits, int sps) {
     size_t smem = (size_t)32 * h->k * sizeof(double);
-    allow_max_smem((const void *)fp64_xty_kernel<MAXC>);
+    DPCA_TRY(allow_max_smem((const void *)fp64_xty_kernel<MAXC>));
     dim3 grid(ceil_div(h->n_ind, 128), splits);
     fp64_xty_kernel<MAXC><<<grid, 512, smem, h->stream>>>(h->P, h->pitch, h->lut, h->n_ind, h->n_snp, h->k, y,
                                                            h->partial, sps);
+    return DPCA_OK;
 }
 
 dpca_status launch_fp64_xty(Handle *h, const double *y, double *z) {
@@ -185,10 +187,10 @@ dpca_status launch_fp64_xty(Handle *h, const double *y, double *z) {
     {
         ScopedLaunch t(&h->clock, h->stream, "fp64_xty");
         int mc = (h->k + 3) / 4;
-        if (mc <= 4) xty_launch<4>(h, y, splits, sps);
-        else if (mc <= 8) xty_launch<8>(h, y, splits, sps);
-        else if (mc <= 16) xty_launch<16>(h, y, splits, sps);
-        else xty_launch<32>(h, y, splits, sps);
+        if (mc <= 4) DPCA_TRY(xty_launch<4>(h, y, splits, sps));
+        else if (mc <= 8) DPCA_TRY(xty_launch<8>(h, y, splits, sps));
+        else if (mc <= 16) DPCA_TRY(xty_launch<16>(h, y, splits, sps));
+        else DPCA_TRY(xty_launch<32>(h, y, splits, sps));
         DPCA_CUDA(cudaGetLastError());
     }
     {
@@ -216,7 +218,10 @@ namespace dpca {
 //
 // In host code the array's name is only a host-side stand-in: its device address is obtained
 // once per device, with that device current, by cudaGetSymbolAddress on the first call made on
-// that device (so that first call should come before any stream capture).  Every call shares
+// that device, which also raises the shared-memory limits of every kernel instance the call may
+// launch (so that first call should come before any stream capture).  The address belongs to the
+// CUDA context it was looked up in; a call in another context (for instance after
+// cudaDeviceReset) repeats this set-up, and that call too belongs outside capture.  Every call shares
 // the array and it keeps the last call's contents; nothing in it needs to start at zero (each
 // kernel writes every element it later reads).  Calls whose work overlaps on the GPU -- on
 // different streams or from different threads -- race on the array, so callers serialise them.
@@ -225,10 +230,27 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
+// Device address of the scratch array in the calling thread's current CUDA context.  The address
+// belongs to that context: it is looked up again (cudaGetSymbolAddress) whenever the context id
+// differs from the one it was cached for -- another device, a context the caller made current,
+// or the new primary context after cudaDeviceReset -- and the kernels' shared-memory limits
+// are raised in the same one-time set-up, so that no later call changes a kernel attribute.
 static std::mutex g_noalloc_mu;
-static void *g_noalloc_ptr[kNoAllocMaxDevices];
+struct NoAllocSlot {
+    unsigned long long ctx = 0;
+    void *ptr = nullptr;
+};
+static NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices];
 
-// Device address of the scratch array on the current device (set up on first use).
+static dpca_status noalloc_kernel_setup() {
+    const void *fns[] = {(const void *)fp64_xw_kernel<4>,   (const void *)fp64_xw_kernel<8>,
+                         (const void *)fp64_xw_kernel<16>,  (const void *)fp64_xw_kernel<32>,
+                         (const void *)fp64_xty_kernel<4>,  (const void *)fp64_xty_kernel<8>,
+                         (const void *)fp64_xty_kernel<16>, (const void *)fp64_xty_kernel<32>};
+    for (const void *f : fns) DPCA_TRY(allow_max_smem(f));
+    return DPCA_OK;
+}
+
 static dpca_status noalloc_scratch(void **out) {
     int dev = 0;
     DPCA_CUDA(cudaGetDevice(&dev));
@@ -236,8 +258,11 @@ static dpca_status noalloc_scratch(void **out) {
         set_error("allocation-free pass: device ordinal %d is above %d", dev, kNoAllocMaxDevices - 1);
         return DPCA_ERR_UNSUPPORTED;
     }
+    unsigned long long ctx = 0;
+    DPCA_TRY(current_context_id(&ctx));
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoAllocSlot &slot = g_noalloc_slot[dev];
+    if (slot.ctx != ctx || !slot.ptr) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -245,29 +270,55 @@ static dpca_status noalloc_scratch(void **out) {
                       cudaGetErrorString(e));
             return DPCA_ERR_CUDA;
         }
-        g_noalloc_ptr[dev] = p;
+        DPCA_TRY(noalloc_kernel_setup());
+        slot.ctx = ctx;
+        slot.ptr = p;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = slot.ptr;
     return DPCA_OK;
 }
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 template <int MAXC>
-static void xw_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
-                          const double *omega, double *y, cudaStream_t st) {
+static dpca_status xw_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
+                                 const double *omega, double *y, cudaStream_t st) {
     size_t smem = (size_t)64 * k * sizeof(double);
-    allow_max_smem((const void *)fp64_xw_kernel<MAXC>);
+    DPCA_TRY(allow_max_smem((const void *)fp64_xw_kernel<MAXC>));
     fp64_xw_kernel<MAXC><<<ceil_div(n_snp, 64), 256, smem, st>>>(P, pitch, lut, n_ind, n_snp, k, omega, y);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
 }
 
 template <int MAXC>
-static void xty_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
-                           const double *y, double *partial, int splits, int sps, cudaStream_t st) {
+static dpca_status xty_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
+                                  const double *y, double *partial, int splits, int sps, cudaStream_t st) {
     size_t smem = (size_t)32 * k * sizeof(double);
-    allow_max_smem((const void *)fp64_xty_kernel<MAXC>);
+    DPCA_TRY(allow_max_smem((const void *)fp64_xty_kernel<MAXC>));
     dim3 grid(ceil_div(n_ind, 128), splits);
     fp64_xty_kernel<MAXC><<<grid, 512, smem, st>>>(P, pitch, lut, n_ind, n_snp, k, y, partial, sps);
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
+// Both products' launchers for the subspace width k (the kernel instance covers ceil(k / 4) column
+// groups of four).
+static dpca_status xw_dispatch(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
+                               const double *omega, double *y, cudaStream_t st) {
+    const int mc = (k + 3) / 4;
+    if (mc <= 4) return xw_launch_raw<4>(P, pitch, lut, n_ind, n_snp, k, omega, y, st);
+    if (mc <= 8) return xw_launch_raw<8>(P, pitch, lut, n_ind, n_snp, k, omega, y, st);
+    if (mc <= 16) return xw_launch_raw<16>(P, pitch, lut, n_ind, n_snp, k, omega, y, st);
+    return xw_launch_raw<32>(P, pitch, lut, n_ind, n_snp, k, omega, y, st);
+}
+
+static dpca_status xty_dispatch(const uint8_t *P, int64_t pitch, const double *lut, int n_ind, int n_snp, int k,
+                                const double *y, double *partial, int splits, int sps, cudaStream_t st) {
+    const int mc = (k + 3) / 4;
+    if (mc <= 4) return xty_launch_raw<4>(P, pitch, lut, n_ind, n_snp, k, y, partial, splits, sps, st);
+    if (mc <= 8) return xty_launch_raw<8>(P, pitch, lut, n_ind, n_snp, k, y, partial, splits, sps, st);
+    if (mc <= 16) return xty_launch_raw<16>(P, pitch, lut, n_ind, n_snp, k, y, partial, splits, sps, st);
+    return xty_launch_raw<32>(P, pitch, lut, n_ind, n_snp, k, y, partial, splits, sps, st);
 }
 
 // One streamed block of the FP64 pass: Y_b = X_b Omega into h->y (blk x k), then
@@ -275,14 +326,10 @@ static void xty_launch_raw(const uint8_t *P, int64_t pitch, const double *lut, i
 dpca_status launch_fp64_block(Handle *h, int b, int s0, int ns, const double *omega, double *z, bool accumulate) {
     const uint8_t *P = h->Pb[b];
     const double *lut = h->lut + 4 * (size_t)s0;
-    const int k = h->k, mc = (k + 3) / 4;
+    const int k = h->k;
     {
         ScopedLaunch t(&h->clock, h->stream, "fp64_xw");
-        if (mc <= 4) xw_launch_raw<4>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
-        else if (mc <= 8) xw_launch_raw<8>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
-        else if (mc <= 16) xw_launch_raw<16>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
-        else xw_launch_raw<32>(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream);
-        DPCA_CUDA(cudaGetLastError());
+        DPCA_TRY(xw_dispatch(P, h->pitch, lut, h->n_ind, ns, k, omega, h->y, h->stream));
     }
     const int tiles = ceil_div(h->n_ind, 128);
     int splits = std::max(1, ceil_div(4 * h->sm_count, tiles));
@@ -293,11 +340,7 @@ dpca_status launch_fp64_block(Handle *h, int b, int s0, int ns, const double *om
     splits = ceil_div(ns, sps);
     {
         ScopedLaunch t(&h->clock, h->stream, "fp64_xty");
-        if (mc <= 4) xty_launch_raw<4>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
-        else if (mc <= 8) xty_launch_raw<8>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
-        else if (mc <= 16) xty_launch_raw<16>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
-        else xty_launch_raw<32>(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream);
-        DPCA_CUDA(cudaGetLastError());
+        DPCA_TRY(xty_dispatch(P, h->pitch, lut, h->n_ind, ns, k, h->y, h->partial, splits, sps, h->stream));
     }
     ScopedLaunch t(&h->clock, h->stream, "reduce_splits");
     const int64_t elems = (int64_t)h->n_ind * k;
@@ -364,15 +407,9 @@ extern "C" dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row
     cudaStream_t st = (cudaStream_t)stream;
     launch_snp_stats_raw(packed, row_stride, n_ind, n_snp, 1.0 / sqrt((double)n_snp), counts, avg, sd, lut, nullptr,
                          st);
-    const int mc = (nrhs + 3) / 4;
-    if (mc <= 4) xw_launch_raw<4>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
-    else if (mc <= 8) xw_launch_raw<8>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
-    else if (mc <= 16) xw_launch_raw<16>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
-    else xw_launch_raw<32>(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st);
-    if (mc <= 4) xty_launch_raw<4>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
-    else if (mc <= 8) xty_launch_raw<8>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
-    else if (mc <= 16) xty_launch_raw<16>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
-    else xty_launch_raw<32>(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st);
+    DPCA_CUDA(cudaGetLastError());
+    DPCA_TRY(xw_dispatch(packed, row_stride, lut, n_ind, n_snp, nrhs, omega, y, st));
+    DPCA_TRY(xty_dispatch(packed, row_stride, lut, n_ind, n_snp, nrhs, y, partial, splits, sps, st));
     const int64_t elems = (int64_t)n_ind * nrhs;
     const int grid = (int)std::min<int64_t>((elems + 255) / 256, (int64_t)sm_count * 8);
     reduce_splits_kernel<<<grid, 256, 0, st>>>(partial, elems, splits, z);

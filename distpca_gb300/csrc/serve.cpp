@@ -8,8 +8,10 @@
 // stream-ordered allocation of a resident handle, upload (or on-device synthesis) of the packed
 // rows with their per-SNP statistics, the start block, the solve, and stream-ordered release.
 // Jobs in flight overlap on the device kernel by kernel; no job's allocation or release waits for
-// another job's work, because every device buffer comes from the device's memory pool on the
-// job's own stream and the pool may not make one stream wait for another to reuse memory.
+// another job's work, because every device buffer comes from the server's own memory pool on the
+// job's own stream and the pool may not make one stream wait for another to reuse memory.  The
+// pool belongs to the server (created with it, destroyed at shutdown), so the device's default
+// pool, which other code in the process may use, keeps its settings and its memory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -53,6 +55,7 @@ struct dpca_server {
     std::unordered_map<int64_t, Job *> jobs;
     std::vector<std::thread> workers;
     std::vector<cudaStream_t> streams;
+    cudaMemPool_t pool = nullptr;
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -108,7 +111,8 @@ dpca_status run_job(dpca_server *s, Job *j, cudaStream_t stream) {
     const dpca_job &q = j->spec;
     DPCA_CUDA(cudaSetDevice(s->device));
     dpca_handle *hh = nullptr;
-    dpca_status st = create_serving_handle(&hh, q.n_ind, q.n_snp, q.cfg.nrhs, q.cfg.precision, s->device, stream);
+    dpca_status st =
+        create_serving_handle(&hh, q.n_ind, q.n_snp, q.cfg.nrhs, q.cfg.precision, s->device, stream, s->pool);
     if (st == DPCA_OK) {
         if (q.packed)
             st = dpca_upload(hh, q.packed, q.row_stride);
@@ -217,16 +221,30 @@ dpca_status dpca_serve_create(dpca_server **out, const dpca_serve_config *cfg) {
     DPCA_CUDA(cudaSetDevice(cfg->device));
     size_t free_b = 0, total_b = 0;
     DPCA_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    // The device's default pool serves every job: keep freed memory in the pool (no release to
-    // the driver at synchronisations) and never let one stream wait for another's frees.
-    cudaMemPool_t pool;
-    DPCA_CUDA(cudaDeviceGetDefaultMemPool(&pool, cfg->device));
+    // The server's own pool serves every job: it keeps freed memory (no release to the driver at
+    // synchronisations) and never lets one stream wait for another's frees.
+    cudaMemPool_t pool = nullptr;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = cfg->device;
+    DPCA_CUDA(cudaMemPoolCreate(&pool, &props));
     uint64_t keep = UINT64_MAX;
     int no = 0;
-    DPCA_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
-    DPCA_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no));
+    if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess ||
+        cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no) != cudaSuccess) {
+        cudaGetLastError();
+        cudaMemPoolDestroy(pool);
+        set_error("dpca_serve_create: memory pool attributes refused");
+        return DPCA_ERR_CUDA;
+    }
     dpca_server *s = new (std::nothrow) dpca_server();
-    if (!s) return DPCA_ERR_NOMEM;
+    if (!s) {
+        cudaMemPoolDestroy(pool);
+        return DPCA_ERR_NOMEM;
+    }
+    s->pool = pool;
     s->device = cfg->device;
     s->slots = slots;
     s->budget = cfg->hbm_budget_gb > 0 ? (size_t)(cfg->hbm_budget_gb * 1e9) : (size_t)(0.85 * (double)free_b);
@@ -236,6 +254,7 @@ dpca_status dpca_serve_create(dpca_server **out, const dpca_serve_config *cfg) {
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
             cudaGetLastError();
             for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
+            cudaMemPoolDestroy(s->pool);
             delete s;
             set_error("dpca_serve_create: stream creation failed");
             return DPCA_ERR_CUDA;
@@ -340,8 +359,9 @@ dpca_status dpca_serve_shutdown(dpca_server *s) {
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
     }
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    // every job's buffers went back to the pool on its (now idle) stream: destroying the pool
+    // returns its memory to the driver
+    if (s->pool) cudaMemPoolDestroy(s->pool);
     for (auto &kv : s->jobs) delete kv.second;
     delete s;
     return DPCA_OK;

@@ -191,7 +191,8 @@ dpca_status dpca_kernel_times(dpca_handle *h, char *names, size_t names_cap, dou
                               int *count, int cap);
 dpca_status dpca_reset_kernel_times(dpca_handle *h, int enable);
 
-/* ---- unit-parity entry: decode + counts for packed rows in host memory ---- */
+/* ---- unit-parity entry: decode + counts for packed rows in host memory, on the calling
+ * thread's current CUDA device ---- */
 dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp, int32_t *counts,
                                double *avg, double *sd);
 
@@ -212,8 +213,12 @@ dpca_status dpca_decode_counts(const uint8_t *packed, int64_t row_stride, int n_
  * library holds until the process exits; inputs whose statistics, Y and one split of partial
  * sums do not fit (about 64 + 8*nrhs bytes per SNP plus 8*nrhs bytes per individual) are
  * rejected with DPCA_ERR_UNSUPPORTED before any work is queued.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress), so make that first call before
- * any stream capture.  All calls share the array: calls whose work overlaps on the GPU race on
+ * looks up the array's device address (cudaGetSymbolAddress) and raises the shared-memory limit
+ * of every kernel the entry point may launch, so make that first call before any stream
+ * capture.  The address belongs to the CUDA context current at that call; a call in a different
+ * context (another context the caller made current, or the device's new primary context after
+ * cudaDeviceReset) repeats the set-up, so the first call after such a change also belongs
+ * outside capture.  All calls share the array: calls whose work overlaps on the GPU race on
  * it, so serialise them (one stream, or events between streams). */
 dpca_status dpca_pass_fp64_noalloc(const uint8_t *packed, int64_t row_stride, int n_ind, int n_snp,
                                    const double *omega, int nrhs, double *z, void *stream);

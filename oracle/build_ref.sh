@@ -9,12 +9,25 @@
 # MPI is replaced by oracle/shim/mpi.h (one rank, pread for MPI-IO) and
 # MKL/OpenBLAS by scipy's bundled OpenBLAS through oracle/shim/*.h.
 # Flags follow the reference Makefile's Linux branch (-O3, no -fopenmp).
+#
+# The checkout is $DPCA_REFERENCE, else the one this recipe was written against.  Options:
+#   --if-present   exit 0 without building when the checkout is absent (the GPU machine has none)
+#   --print-ref    print the checkout directory and exit (scripts that read the reference's
+#                  files, such as tests/golden/make_golden.py, ask this recipe for it)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${DPCA_REFERENCE:-/root/reference}"
 OUT="$HERE/_ref"
 SRC="$REF/src"
+if [ "${1:-}" = "--print-ref" ]; then
+    echo "$REF"
+    exit 0
+fi
 if [ ! -f "$SRC/methods.cpp" ]; then
+    if [ "${1:-}" = "--if-present" ]; then
+        echo "build_ref.sh: no reference checkout at $REF; oracle/_ref not built"
+        exit 0
+    fi
     echo "build_ref.sh: reference sources not found under $REF" >&2
     exit 1
 fi

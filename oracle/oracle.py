@@ -43,13 +43,16 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+def reference_dir() -> str:
+    """The reference checkout that build_ref.sh reads (it may not exist on this machine)."""
+    out = subprocess.check_output(["bash", os.path.join(HERE, "build_ref.sh"), "--print-ref"])
+    return out.decode().strip()
+
+
 def build_reference() -> Optional[str]:
-    """Build oracle/_ref from the reference sources when they are present."""
-    ref = os.environ.get("DPCA_REFERENCE", "/root/reference")
-    if not os.path.exists(os.path.join(ref, "src", "methods.cpp")):
-        return None
-    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
-    return REF_EXE
+    """Build oracle/_ref from the reference sources when they are present (None otherwise)."""
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh"), "--if-present"])
+    return REF_EXE if os.path.exists(REF_EXE) else None
 
 
 class OracleCfg(ctypes.Structure):

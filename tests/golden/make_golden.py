@@ -11,7 +11,7 @@ that oracle/build_ref.sh builds from the reference sources:
 Everything lands in golden.npz and *_ref_*.txt next to this script.
 
 Run from the repository root:  python tests/golden/make_golden.py
-Needs the reference checkout (DPCA_REFERENCE, default /root/reference).
+Needs the reference checkout that oracle/build_ref.sh reads (DPCA_REFERENCE overrides it).
 """
 from __future__ import annotations
 

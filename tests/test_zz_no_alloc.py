@@ -61,6 +61,40 @@ def test_no_alloc_pass_matches_handle_pass_twice(dpca):
         assert rel_max(z, zr) < TOL, (call, rel_max(z, zr))
 
 
+def test_no_alloc_pass_wide_block_and_single_split(dpca):
+    """nrhs 128 (the widest block: 64 KB of dynamic shared memory in the X Omega kernel, above the
+    default 48 KB limit) on a shape that leaves room for exactly one split of X^T Y partials in
+    the 32 MiB array (28,000 SNPs x 128 columns of Y plus per-SNP statistics take ~30.5 MB, one
+    split of 2,000 x 128 partials 2 MB), twice in a row."""
+    torch = pytest.importorskip("torch")
+    from distpca_gb300 import synth
+
+    n_ind, n_snp, k = 2000, 28_000, 128
+    fixed = 4 * n_snp * 4 + 2 * n_snp * 8 + 4 * n_snp * 8 + n_snp * k * 8
+    part = n_ind * k * 8
+    assert fixed + part <= 32 << 20 < fixed + 2 * part  # one split fits, two do not
+    c = synth.make_cohort(n_ind, n_snp, n_pop=4, fst=0.05, missing=0.02, seed=23)
+    packed = synth.pack_rows(c)
+    stride = (packed.shape[1] + 31) // 32 * 32
+    padded = np.zeros((n_snp, stride), dtype=np.uint8)
+    padded[:, :packed.shape[1]] = packed
+    dev = torch.device("cuda:0")
+    d_packed = torch.from_numpy(padded).to(dev)
+    d_z = torch.empty((n_ind, k), dtype=torch.float64, device=dev)
+    L = dpca.lib()
+    rng = np.random.default_rng(7)
+    for call in range(2):
+        om = rng.standard_normal((n_ind, k))
+        d_om = torch.from_numpy(om).to(dev)
+        st = L.dpca_pass_fp64_noalloc(ctypes.c_void_p(d_packed.data_ptr()), stride, n_ind, n_snp,
+                                      ctypes.c_void_p(d_om.data_ptr()), k, ctypes.c_void_p(d_z.data_ptr()), None)
+        assert st == 0, L.dpca_last_error()
+        torch.cuda.synchronize(dev)
+        z = d_z.cpu().numpy()
+        zr = handle_pass(dpca, packed, n_ind, om)
+        assert rel_max(z, zr) < TOL, (call, rel_max(z, zr))
+
+
 def test_no_alloc_pass_rejects_sizes_beyond_its_scratch(dpca):
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda:0")
