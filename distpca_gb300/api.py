@@ -92,6 +92,8 @@ _SIGS = {
                                            ctypes.POINTER(ctypes.c_int)]),
     "dpca_start_block": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "dpca_sym_eig": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dpca_sym_eig_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
     "dpca_run": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(Result)]),
     "dpca_run_packed": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(Result)]),
@@ -221,14 +223,18 @@ def start_block(n_ind: int, k: int) -> np.ndarray:
     return out
 
 
-def sym_eig(b: np.ndarray):
+def sym_eig(b: np.ndarray, device: Optional[int] = None):
     """Eigenvalues (descending) and eigenvectors (columns) of the symmetric matrix b (upper triangle
-    used): the solve's Rayleigh-Ritz eigenproblem, computed on the host."""
+    used): the Rayleigh-Ritz eigenproblem, on the host (dsyev's method), or with the device kernel
+    the solve uses when `device` is given."""
     b = np.ascontiguousarray(b, dtype=np.float64)
     k = b.shape[0]
     w = np.empty(k)
     W = np.empty((k, k))
-    _check(lib().dpca_sym_eig(k, _p(b), _p(w), _p(W)))
+    if device is None:
+        _check(lib().dpca_sym_eig(k, _p(b), _p(w), _p(W)))
+    else:
+        _check(lib().dpca_sym_eig_device(device, k, _p(b), _p(w), _p(W)))
     return w, W
 
 

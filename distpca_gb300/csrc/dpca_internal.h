@@ -184,7 +184,6 @@ dpca_status launch_qr(Handle *h, double *a);
 dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, double *out);  // k x k = A^T B
 dpca_status launch_eig_desc(Handle *h);                                                   // small.B -> W, w
 dpca_status host_sym_eig_desc(int k, const double *B, double *w, double *W);              // eig_host.cpp
-void host_chol_inv(int k, int n, const double *G, bool shift, double *Rinv);               // eig_host.cpp
 dpca_status launch_apply_w(Handle *h, const double *q, double *out);                      // out = Q W
 dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol, int ii, const double *old,
                                        const double *omega);
@@ -217,7 +216,9 @@ dpca_status launch_mixed_xty(Handle *h, double *z);
 
 // host-side helpers shared between translation units
 dpca_status handle_pass(Handle *h);
-dpca_status check_device_flag(Handle *h);  // DPCA_ERR_TIMEOUT when a bounded device wait gave up
+// Reads the device flags (synchronises the stream): DPCA_ERR_TIMEOUT when a bounded device wait
+// gave up (flag 0), DPCA_ERR_NUMERIC when a device k x k solve did not converge (flag 1).
+dpca_status check_device_flag(Handle *h);
 bool env_flag(const char *name);
 
 }  // namespace dpca

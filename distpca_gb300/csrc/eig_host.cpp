@@ -1,17 +1,12 @@
-// The Rayleigh-Ritz eigenproblem on the host: the k x k symmetric matrix B = Q^T Z (k <= 128)
-// -> eigenvalues in descending order and their eigenvectors, the result of the reference's
-// LAPACKE_dsyev('V', 'U') followed by its column reversal (methods.cpp:981-1000).
-//
-// Why the host: the problem is tiny (k^3 ~ 1e5 flops) and sequential, and this GPU's FP64
-// rate on the one SM such a solve can use is a few flops per cycle, so a device Jacobi solve of
-// k = 40 took ~1.3 ms; a CPU core does it in tens of microseconds.  The matrix comes over with
-// one stream synchronisation per outer iteration.
+// The k x k symmetric eigenproblem on the host: B (k <= 128, upper triangle used) -> eigenvalues
+// in descending order and their eigenvectors, the result of LAPACKE_dsyev('V', 'U') followed by
+// the reference's column reversal (methods.cpp:981-1000).  This is dpca_sym_eig, a host-side
+// utility of the C ABI (the solve itself runs its Rayleigh-Ritz step on the device, k_dense.cu).
 //
 // Method (as dsyev): Householder reduction to tridiagonal form with the orthogonal factor
 // accumulated, then the implicit symmetric QR algorithm with Wilkinson shifts (Golub & Van Loan,
 // Matrix Computations, 4th ed., Algorithms 8.3.1 and 8.3.3), eigenvectors accumulated from the
-// Givens rotations.  Backward stable; eigenvector signs are those the iteration produces (the
-// solve's outputs are defined up to column sign, as the reference's are across LAPACK builds).
+// Givens rotations.  Backward stable; eigenvector signs are those the iteration produces.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -125,51 +120,6 @@ dpca_status host_sym_eig_desc(int k, const double *B, double *w, double *W) {
         for (int i = 0; i < n; ++i) W[(size_t)i * n + c] = Q[(size_t)i * n + ord[c]];
     }
     return DPCA_OK;
-}
-
-// R^-1 of the Cholesky factor of G (+ shift I), both k x k row-major (upper triangle of R^-1,
-// zeros below): one step of the shifted CholeskyQR3 (k_dense.cu launch_qr).  The shift
-// 11 (n k + k (k + 1)) u trace(G) is applied when `shift` is set or when a plain factorization
-// meets a non-positive pivot; a pivot that still fails is replaced by 1 (a zero or non-finite
-// column stays unnormalised instead of dividing by zero).
-void host_chol_inv(int k, int n, const double *G, bool shift, double *Rinv) {
-    std::vector<double> R((size_t)k * k);
-    double tr = 0.0;
-    for (int i = 0; i < k; ++i) tr += G[(size_t)i * k + i];
-    const double s = 11.0 * ((double)n * k + (double)k * (k + 1)) * std::ldexp(1.0, -53) * tr;
-    for (int attempt = shift ? 1 : 0; attempt < 2; ++attempt) {
-        bool broke = false;
-        for (int i = 0; i < k; ++i)
-            for (int j = 0; j < k; ++j) R[(size_t)i * k + j] = G[(size_t)i * k + j] + (attempt == 1 && i == j ? s : 0.0);
-        for (int j = 0; j < k && !broke; ++j) {
-            double d = R[(size_t)j * k + j];
-            if (!(d > 0.0) || !std::isfinite(d)) {
-                if (attempt == 0) {
-                    broke = true;
-                    break;
-                }
-                d = 1.0;
-            }
-            const double r = std::sqrt(d), inv = 1.0 / r;
-            R[(size_t)j * k + j] = r;
-            for (int c = j + 1; c < k; ++c) R[(size_t)j * k + c] *= inv;
-            for (int a = j + 1; a < k; ++a) {
-                const double rja = R[(size_t)j * k + a];
-                for (int c = a; c < k; ++c) R[(size_t)a * k + c] -= rja * R[(size_t)j * k + c];
-            }
-        }
-        if (!broke) break;
-    }
-    // R^-1 by back substitution, column by column
-    for (int i = 0; i < k * k; ++i) Rinv[i] = 0.0;
-    for (int c = 0; c < k; ++c) {
-        Rinv[(size_t)c * k + c] = 1.0 / R[(size_t)c * k + c];
-        for (int i = c - 1; i >= 0; --i) {
-            double sum = 0.0;
-            for (int l = i + 1; l <= c; ++l) sum += R[(size_t)i * k + l] * Rinv[(size_t)l * k + c];
-            Rinv[(size_t)i * k + c] = -sum / R[(size_t)i * k + i];
-        }
-    }
 }
 
 }  // namespace dpca

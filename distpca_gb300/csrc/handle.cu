@@ -440,6 +440,11 @@ dpca_status check_device_flag(Handle *h) {
         cudaMemsetAsync(h->dflag, 0, 16 * sizeof(int), h->stream);
         return DPCA_ERR_TIMEOUT;
     }
+    if (flags[1]) {
+        set_error("a device k x k solve did not converge (site %d)", flags[1]);
+        cudaMemsetAsync(h->dflag, 0, 16 * sizeof(int), h->stream);
+        return DPCA_ERR_NUMERIC;
+    }
     return DPCA_OK;
 }
 

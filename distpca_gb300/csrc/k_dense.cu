@@ -1,13 +1,16 @@
-// Small dense FP64 steps of the subspace iteration (methods.cpp:944-1063):
+// Small dense FP64 steps of the subspace iteration (methods.cpp:944-1063), all on the device:
 //   launch_qr         thin QR of the n x k panel by shifted CholeskyQR3: atb_kernel (Gram),
-//                     the k x k Cholesky factor's inverse on the host (eig_host.cpp), and
+//                     chol_inv_kernel (the k x k Cholesky factor and its inverse, one block) and
 //                     apply_w_kernel (A R^-1), three times (methods.cpp:947-961, see launch_qr).
 //   atb_kernel        C = A^T B over the n rows (B = Q^T Z, methods.cpp:972-973; the in-core
 //                     Gram (XQ)^T (XQ), methods.cpp:141-142).
-//   launch_eig_desc   the k x k eigenproblem (dsyev 'V','U', methods.cpp:981-1000) on the host.
+//   launch_eig_desc   the k x k eigenproblem (dsyev 'V','U' and the column reversal,
+//                     methods.cpp:981-1000): sym_eig_kernel, parallel cyclic Jacobi in one block.
 //   apply_w_kernel    Omega = Q W (methods.cpp:1006-1007).
 //   coldots_kernel + criterion_kernel: sigma = sqrt(w), sum, and crit 0/1/2
 //                     (methods.cpp:1012-1063).
+// None of them synchronises with the host: the solve reads results back once per outer
+// iteration (the criterion), so the host enqueues a whole iteration ahead of the device.
 #include <algorithm>
 #include <cmath>
 
@@ -104,19 +107,144 @@ dpca_status launch_atb(Handle *h, const double *a, const double *b, int n, doubl
     return atb_timed(h, a, b, n, out, "atb", "atb_sum");
 }
 
-// The k x k eigenproblem goes to the host (eig_host.cpp): B down, W and w (adjacent in the small
-// block) back up.  The event pair brackets the copies and the host solve.
+// ------------------------------------------------------------------ k x k eigenproblem
+// The Rayleigh-Ritz matrix B (k x k, upper triangle used, as dsyev 'U') -> eigenvalues w in
+// descending order and eigenvectors W (row-major, column c belongs to w[c]): one block, cyclic
+// Jacobi with the round-robin ordering, in which each round rotates k/2 disjoint index pairs at
+// once (Golub & Van Loan, Matrix Computations, 4th ed., section 8.5.5, parallel Jacobi).  A round
+// is three barrier-separated steps: the k/2 rotations (one thread each: theta = (a_qq - a_pp) /
+// 2 a_pq, t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)), c = 1 / sqrt(t^2 + 1), s = t c), the
+// row update A <- J^T A over every (pair, column), and the column update A <- A J, V <- V J over
+// every (pair, row), which also zeroes the annihilated entries.  A pair is skipped when
+// |a_pq| <= eps/2 sqrt(|a_pp a_qq|), the relative criterion under which Jacobi keeps the
+// eigenvalues of a positive semi-definite matrix (B = Q^T X^T X Q is one) to high relative
+// accuracy; the solve stops after the first sweep that rotates nothing.  From the second outer
+// iteration on, B is nearly diagonal (the previous Ritz vectors are the start block), and Jacobi
+// converges quadratically from there: two or three sweeps.
+//
+// Why Jacobi and not the tridiagonal QR algorithm dsyev runs: every step here is k/2 or k^2/2
+// independent updates, where the tridiagonal bulge chase is one long chain of dependent FP64
+// operations, and a single thread's dependent FP64 chain is what this GPU does slowest.  Both are
+// backward stable; the eigenvectors' signs are arbitrary in both (the outputs are defined up to
+// column sign, as the reference's are across LAPACK builds).
+constexpr int kEigThreads = 256;
+constexpr int kEigMaxSweeps = 60;
+constexpr int kEigSmemK = 112;  // A and V both in shared memory up to this k (2 k^2 doubles)
+
+__host__ __device__ inline size_t eig_smem_bytes(int k) {
+    return (size_t)(k <= kEigSmemK ? 2 : 1) * k * k * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const double *__restrict__ Bin, int k,
+                                                              double *__restrict__ Wout, double *__restrict__ wout,
+                                                              double *__restrict__ vglobal, int *__restrict__ err) {
+    extern __shared__ double esm[];
+    __shared__ double cs[64], sn[64], dg[128];
+    __shared__ int pp[64], qq[64], ord[128];
+    __shared__ int rotated;
+    double *A = esm;
+    double *V = k <= kEigSmemK ? esm + k * k : vglobal;
+    const int tid = threadIdx.x, kk2 = k * k;
+    const int kk = k + (k & 1), npairs = kk / 2;
+    const double eps = 0x1p-52;
+    for (int e = tid; e < kk2; e += kEigThreads) {
+        const int i = e / k, j = e - i * k;
+        A[e] = i <= j ? Bin[e] : Bin[j * k + i];  // the upper triangle, mirrored
+        V[e] = i == j ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    int sweep = 0;
+    for (; sweep < kEigMaxSweeps && k > 1; ++sweep) {
+        if (tid == 0) rotated = 0;
+        __syncthreads();
+        for (int r = 0; r < kk - 1; ++r) {
+            // step 1: the rotations of this round (pair 0 = (0, 1 + r); the others pair positions
+            // r + i and r - i on the circle of the remaining kk - 1 indices)
+            if (tid < npairs) {
+                int p = tid == 0 ? 0 : 1 + (r + tid) % (kk - 1);
+                int q = tid == 0 ? 1 + r % (kk - 1) : 1 + (r - tid + kk - 1) % (kk - 1);
+                if (p > q) {
+                    const int t = p;
+                    p = q;
+                    q = t;
+                }
+                double c = 1.0, s = 0.0;
+                if (q < k) {
+                    const double apq = A[p * k + q], app = A[p * k + p], aqq = A[q * k + q];
+                    if (apq != 0.0 && fabs(apq) > 0.5 * eps * sqrt(fabs(app * aqq))) {
+                        const double theta = (aqq - app) / (2.0 * apq);
+                        double t;
+                        if (fabs(theta) > 1e150) t = 0.5 / theta;
+                        else t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                        c = 1.0 / sqrt(t * t + 1.0);
+                        s = t * c;
+                        if (s != 0.0) rotated = 1;
+                    }
+                }
+                pp[tid] = p;
+                qq[tid] = q;
+                cs[tid] = c;
+                sn[tid] = s;
+            }
+            __syncthreads();
+            // step 2: rows p, q of A for every pair (pairs touch disjoint rows)
+            for (int e = tid; e < npairs * k; e += kEigThreads) {
+                const int i = e / k, j = e - i * k;
+                const double s = sn[i];
+                if (s == 0.0) continue;
+                const double c = cs[i];
+                const int p = pp[i], q = qq[i];
+                const double ap = A[p * k + j], aq = A[q * k + j];
+                A[p * k + j] = c * ap - s * aq;
+                A[q * k + j] = s * ap + c * aq;
+            }
+            __syncthreads();
+            // step 3: columns p, q of A and V; the annihilated pair is set to zero exactly
+            for (int e = tid; e < npairs * k; e += kEigThreads) {
+                const int i = e / k, j = e - i * k;
+                const double s = sn[i];
+                if (s == 0.0) continue;
+                const double c = cs[i];
+                const int p = pp[i], q = qq[i];
+                const double ap = A[j * k + p], aq = A[j * k + q];
+                A[j * k + p] = j == q ? 0.0 : c * ap - s * aq;
+                A[j * k + q] = j == p ? 0.0 : s * ap + c * aq;
+                const double vp = V[j * k + p], vq = V[j * k + q];
+                V[j * k + p] = c * vp - s * vq;
+                V[j * k + q] = s * vp + c * vq;
+            }
+            __syncthreads();
+        }
+        if (!rotated) break;
+        __syncthreads();
+    }
+    if (tid == 0 && sweep >= kEigMaxSweeps) atomicCAS(err + 1, 0, 51);  // not converged
+    // descending order (ties by index): rank of each diagonal entry
+    for (int i = tid; i < k; i += kEigThreads) dg[i] = A[i * k + i];
+    __syncthreads();
+    for (int i = tid; i < k; i += kEigThreads) {
+        int rank = 0;
+        for (int j = 0; j < k; ++j) rank += (dg[j] > dg[i] || (dg[j] == dg[i] && j < i)) ? 1 : 0;
+        ord[rank] = i;
+    }
+    __syncthreads();
+    for (int c = tid; c < k; c += kEigThreads) wout[c] = dg[ord[c]];
+    for (int e = tid; e < kk2; e += kEigThreads) {
+        const int i = e / k, c = e - i * k;
+        Wout[e] = V[i * k + ord[c]];
+    }
+}
+
 dpca_status launch_eig_desc(Handle *h) {
     ScopedLaunch t(&h->clock, h->stream, "sym_eig");
     const int k = h->k;
     const SmallLayout L{k};
-    DPCA_CUDA(cudaMemcpyAsync(h->host_small + L.B(), h->small + L.B(), (size_t)k * k * sizeof(double),
-                              cudaMemcpyDeviceToHost, h->stream));
-    DPCA_CUDA(cudaStreamSynchronize(h->stream));
-    DPCA_TRY(check_device_flag(h));
-    DPCA_TRY(host_sym_eig_desc(k, h->host_small + L.B(), h->host_small + L.w(), h->host_small + L.W()));
-    DPCA_CUDA(cudaMemcpyAsync(h->small + L.W(), h->host_small + L.W(), ((size_t)k * k + k) * sizeof(double),
-                              cudaMemcpyHostToDevice, h->stream));
+    DPCA_TRY(allow_max_smem((const void *)sym_eig_kernel));
+    // V lives in global memory (the reduction scratch, >= k^2 doubles, free at this step) when
+    // A and V do not both fit in shared memory
+    sym_eig_kernel<<<1, kEigThreads, eig_smem_bytes(k), h->stream>>>(h->small + L.B(), k, h->small + L.W(),
+                                                                       h->small + L.w(), h->red, h->dflag);
+    DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
 
@@ -149,6 +277,87 @@ dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
     return DPCA_OK;
 }
 
+// ------------------------------------------------------------------ k x k Cholesky and inverse
+// Rinv = R^-1 of R = chol(G [+ s I]), both k x k row-major (upper triangle, zeros below), in one
+// block: one step of the shifted CholeskyQR3 below.  The shift s = 11 (n k + k (k + 1)) u tr(G) is
+// applied when `shift` is set or when a plain factorization meets a non-positive pivot; a pivot
+// that still fails is replaced by 1 (a zero or non-finite column stays unnormalised instead of
+// dividing by zero).  Right-looking factorization in shared memory (k barrier-separated steps:
+// the pivot, the scaling of its row, the rank-one update of the trailing upper triangle over all
+// threads), then the inverse in place column by column, R^-1[i][j] = -R^-1[j][j] *
+// sum_{l=i..j-1} R^-1[i][l] R[l][j], each row's sum split over a team of lanes.
+constexpr int kCholThreads = 256;
+
+__global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__restrict__ G, int k, int n,
+                                                                int always_shift, double *__restrict__ Rinv) {
+    extern __shared__ double S[];  // k x k
+    __shared__ double pinv[128], col[128];
+    __shared__ double shift;
+    __shared__ int broke;
+    const int tid = threadIdx.x, kk2 = k * k;
+    if (tid == 0) {
+        double tr = 0.0;
+        for (int i = 0; i < k; ++i) tr += G[i * k + i];
+        shift = 11.0 * ((double)n * k + (double)k * (k + 1)) * 0x1p-53 * tr;
+    }
+    for (int attempt = always_shift ? 1 : 0; attempt < 2; ++attempt) {
+        __syncthreads();
+        for (int e = tid; e < kk2; e += kCholThreads) {
+            const int i = e / k, j = e - i * k;
+            S[e] = G[e] + (attempt == 1 && i == j ? shift : 0.0);
+        }
+        if (tid == 0) broke = 0;
+        __syncthreads();
+        for (int j = 0; j < k; ++j) {
+            if (tid == 0) {
+                double d = S[j * k + j];
+                if (!(d > 0.0) || !isfinite(d)) {
+                    if (attempt == 0) broke = 1;
+                    d = 1.0;
+                }
+                const double r = sqrt(d);
+                S[j * k + j] = r;
+                pinv[j] = 1.0 / r;
+            }
+            __syncthreads();
+            if (broke) break;  // block-uniform: read after the barrier
+            const double inv = pinv[j];
+            for (int c = j + 1 + tid; c < k; c += kCholThreads) S[j * k + c] *= inv;
+            __syncthreads();
+            const int m = k - j - 1;
+            for (int e = tid; e < m * m; e += kCholThreads) {
+                const int a = j + 1 + e / m, c = j + 1 + e % m;
+                if (c >= a) S[a * k + c] -= S[j * k + a] * S[j * k + c];
+            }
+            __syncthreads();
+        }
+        if (!broke) break;
+    }
+    // inverse in place: column j of R^-1 from the columns before it (already inverted) and
+    // column j of R (still intact); teams of `tw` lanes (a power of two <= 32) share a row's sum
+    int tw = 1;
+    while (tw < 32 && tw * 2 * k <= kCholThreads) tw *= 2;
+    const int team = tid / tw, lane = tid % tw, teams = kCholThreads / tw;
+    for (int j = 0; j < k; ++j) {
+        for (int i0 = 0; i0 < j; i0 += teams) {
+            const int i = i0 + team;
+            double sum = 0.0;
+            if (i < j)
+                for (int l = i + lane; l < j; l += tw) sum = fma(S[i * k + l], S[l * k + j], sum);
+            for (int o = tw >> 1; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o, tw);
+            if (i < j && lane == 0) col[i] = -sum * pinv[j];
+        }
+        __syncthreads();
+        for (int i = tid; i < j; i += kCholThreads) S[i * k + j] = col[i];
+        if (tid == 0) S[j * k + j] = pinv[j];
+        __syncthreads();
+    }
+    for (int e = tid; e < kk2; e += kCholThreads) {
+        const int i = e / k, j = e - i * k;
+        Rinv[e] = j >= i ? S[e] : 0.0;
+    }
+}
+
 // ------------------------------------------------------------------ shifted CholeskyQR3
 // Thin QR of the n x k panel A (in place, Q only) by three CholeskyQR steps (Fukaya, Kannan,
 // Nakatsukasa, Yamamoto, Yanagisawa, "Shifted Cholesky QR for computing the QR factorization of
@@ -156,32 +365,27 @@ dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
 // A <- A R^-1, with the shift s = 11 (n k + k (k + 1)) u ||A||_F^2 in the first step, which keeps
 // the Cholesky factorization defined for condition numbers up to ~1/u (the reference's start
 // block has ~5e9), and then two plain steps (CholeskyQR2) that restore orthogonality to O(u).
-// The panel is read three times and written three times; no step needs a grid-wide barrier, so
-// the QR costs a dozen short launches instead of ~4k barriers of a column-by-column Householder
-// QR.  Q spans the same column space as the reference's dgeqrf + dorgqr (methods.cpp:947-961);
-// its columns may differ in sign, which the Rayleigh-Ritz step (methods.cpp:972-1007) absorbs:
-// the Ritz vectors come out with the eigensolver's signs either way.
-//
+// The panel is read three times and written three times; no step needs a grid-wide barrier or
+// the host, so the QR is a dozen stream-ordered launches.  Q spans the same column space as the
+// reference's dgeqrf + dorgqr (methods.cpp:947-961); its columns may differ in sign, which the
+// Rayleigh-Ritz step (methods.cpp:972-1007) absorbs: the Ritz vectors come out with the
+// eigensolver's signs either way.
 dpca_status launch_qr(Handle *h, double *a) {
     const int n = h->n_ind, k = h->k;
     const SmallLayout L{k};
     double *G = h->small + L.B(), *Rinv = h->small + L.W();  // free until the Rayleigh-Ritz step
     DPCA_TRY(allow_max_smem((const void *)apply_w_kernel));
+    DPCA_TRY(allow_max_smem((const void *)chol_inv_kernel));
     const size_t smem_g = (size_t)k * k * sizeof(double);
     const int64_t total = (int64_t)n * k;
     const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
     double *src = a, *dst = h->work;
-    // the k x k factorization on the host: a k-step FP64 dependency chain runs ~5x faster on a CPU
-    // core than on the one SM a device launch of it can use (84 us at k = 40, measured)
-    double *hG = h->host_small + L.B(), *hR = h->host_small + L.W();
     for (int step = 0; step < 3; ++step) {
         DPCA_TRY(atb_timed(h, src, src, n, G, "qr_gram", "qr_gram_sum"));
         {
             ScopedLaunch t(&h->clock, h->stream, "qr_chol");
-            DPCA_CUDA(cudaMemcpyAsync(hG, G, (size_t)k * k * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-            DPCA_CUDA(cudaStreamSynchronize(h->stream));
-            host_chol_inv(k, n, hG, step == 0, hR);
-            DPCA_CUDA(cudaMemcpyAsync(Rinv, hR, (size_t)k * k * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            chol_inv_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
+            DPCA_CUDA(cudaGetLastError());
         }
         {
             ScopedLaunch t(&h->clock, h->stream, "qr_apply");
@@ -270,3 +474,49 @@ dpca_status launch_sigma_and_criterion(Handle *h, int nsv, int crit, double tol,
 }
 
 }  // namespace dpca
+
+using namespace dpca;
+
+extern "C" dpca_status dpca_sym_eig_device(int device, int k, const double *b, double *w, double *W) {
+    clear_error();
+    if (k < 1 || k > kMaxNrhs || !b || !w || !W) {
+        set_error("dpca_sym_eig_device: need 1 <= k <= %d and non-null arrays", kMaxNrhs);
+        return DPCA_ERR_INVALID;
+    }
+    DPCA_CUDA(cudaSetDevice(device));
+    const size_t kk = (size_t)k * k;
+    double *d = nullptr;
+    int *flags = nullptr;
+    DPCA_CUDA(cudaMalloc(&d, (3 * kk + k) * sizeof(double)));
+    if (cudaMalloc(&flags, 16 * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d);
+        set_error("dpca_sym_eig_device: device allocation failed");
+        return DPCA_ERR_NOMEM;
+    }
+    dpca_status st = allow_max_smem((const void *)sym_eig_kernel);
+    int hflags[16] = {0};
+    cudaError_t e = cudaSuccess;
+    if (st == DPCA_OK) {
+        // d: B | W | V (global, used for k > kEigSmemK) | w
+        e = cudaMemcpy(d, b, kk * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemset(flags, 0, 16 * sizeof(int));
+        if (e == cudaSuccess) {
+            sym_eig_kernel<<<1, kEigThreads, eig_smem_bytes(k)>>>(d, k, d + kk, d + 3 * kk, d + 2 * kk, flags);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(W, d + kk, kk * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(w, d + 3 * kk, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            set_error("dpca_sym_eig_device: %s", cudaGetErrorString(e));
+            st = DPCA_ERR_CUDA;
+        } else if (hflags[1]) {
+            set_error("dpca_sym_eig_device: Jacobi did not converge");
+            st = DPCA_ERR_NUMERIC;
+        }
+    }
+    cudaFree(d);
+    cudaFree(flags);
+    return st;
+}

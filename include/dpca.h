@@ -128,11 +128,16 @@ dpca_status dpca_probe_bfile(const char *bfile, int *n_ind, int *n_snp);
 dpca_status dpca_resolve_config(dpca_config *cfg, int n_ind, int n_snp, int *rows_fetched);
 /* Start block, bit-identical to the reference RNG loop: n_ind x k row-major. */
 dpca_status dpca_start_block(int n_ind, int k, double *out);
-/* The Rayleigh-Ritz eigenproblem of every outer iteration, on the host (LAPACKE_dsyev 'V','U' and
- * the column reversal, src/methods.cpp:981-1000): b is k x k row-major (upper triangle used);
- * w gets the eigenvalues in descending order, W (k x k row-major) the eigenvectors as columns.
- * Householder tridiagonalization + implicit symmetric QR with Wilkinson shifts. */
+/* The Rayleigh-Ritz eigenproblem (LAPACKE_dsyev 'V','U' and the column reversal,
+ * src/methods.cpp:981-1000) on the host: b is k x k row-major (upper triangle used); w gets the
+ * eigenvalues in descending order, W (k x k row-major) the eigenvectors as columns.  Householder
+ * tridiagonalization + implicit symmetric QR with Wilkinson shifts, dsyev's method.  A host-side
+ * utility: the solve itself runs this step on the device (dpca_sym_eig_device). */
 dpca_status dpca_sym_eig(int k, const double *b, double *w, double *W);
+/* The same eigenproblem with the device kernel every outer iteration of a solve uses (one block,
+ * parallel cyclic Jacobi in FP64, k <= 128), on `device`; b, w, W are host arrays as above.
+ * DPCA_ERR_NUMERIC when it does not converge. */
+dpca_status dpca_sym_eig_device(int device, int k, const double *b, double *w, double *W);
 
 /* ---- whole runs (device) ---- */
 /* Read <bfile>.bed/.bim/.fam and run.  omega_inout: start block in, final Ritz block out. */

@@ -126,3 +126,31 @@ def test_bad_jobs_rejected_at_submission(dpca):
         assert e.value.status == 1
         with pytest.raises(dpca.DpcaError):
             s.submit(c.n_ind, c.n_snp, packed=np.zeros((c.n_snp, 2), np.uint8), **f)  # rows too short
+
+
+def test_jobs_match_oracle(dpca, oracle):
+    """Three jobs of the mixed stream (one FP64, two mixed) against the CPU oracle (the reference's
+    algorithm restated in C, pinned to the reference build) solving the same rows with the same
+    flags and start block: eigenvalues within 1e-10 (FP64) / 1e-6 (mixed) relative, the largest
+    principal angle between the nsv-dimensional subspaces within 1e-6 / 1e-4 rad, iteration
+    counts equal (FP64) or within one (mixed).  The jobs stop at MEV tol 1e-3 after at most six
+    iterations, so their trailing directions still carry the rounding noise of the reference's
+    nearly rank-deficient start block (3.7e-8 rad measured for the FP64 job)."""
+    from distpca_gb300 import synth
+
+    jobs = [cohorts()[i] for i in (0, 1, 3)]
+    packs = [synth.pack_rows(c) for c, _ in jobs]
+    with dpca.Server(slots=3) as s:
+        ids = [s.submit(c.n_ind, c.n_snp, packed=p, **f) for (c, f), p in zip(jobs, packs)]
+        got = [s.result(j) for j in ids]
+    for (c, f), p, r in zip(jobs, packs, got):
+        ref = oracle.solve(p, c.n_ind, nsv=f["nsv"], nrhs=f["nrhs"], power=f["power"], crit=f["crit"], tol=f["tol"],
+                           miter=f["miter"], bsize=f["bsize"])
+        fp64 = f["precision"] == "fp64"
+        lam, lam_r = r["sigma"] ** 2, ref["sigma"] ** 2
+        assert np.max(np.abs(lam - lam_r) / lam_r) < (1e-10 if fp64 else 1e-6)
+        qa, _ = np.linalg.qr(r["u"])
+        qb, _ = np.linalg.qr(ref["u"])
+        ang = float(np.arccos(np.clip(np.linalg.svd(qa.T @ qb, compute_uv=False).min(), -1, 1)))
+        assert ang < (1e-6 if fp64 else 1e-4), ang
+        assert abs(r["its"] - ref["its"]) <= (0 if fp64 else 1), (r["its"], ref["its"])

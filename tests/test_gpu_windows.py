@@ -85,3 +85,36 @@ def test_windows_other_criteria(dpca, crit, tol):
         assert np.max(np.abs(r["sigma"][i] ** 2 - ref["sigma"] ** 2) / ref["sigma"] ** 2) < 1e-6
         assert r["its"][i] == ref["its"]
 
+
+
+def max_angle(u, ref):
+    qa, _ = np.linalg.qr(u)
+    qb, _ = np.linalg.qr(ref)
+    s = np.linalg.svd(qa.T @ qb, compute_uv=False)
+    return float(np.arccos(np.clip(s.min(), -1.0, 1.0)))
+
+
+def test_windows_match_oracle(dpca, oracle):
+    """Three windows of uneven width against the CPU oracle (the reference's algorithm restated in
+    C, pinned to the reference build) solving each window's rows alone: a window is its own PCA,
+    standardized with 1/sqrt(width), so the oracle's solve of those rows is the reference result
+    for it.  Mixed-path gates: eigenvalues within 1e-6 relative, the largest principal angle
+    between the nsv-dimensional subspaces within 1e-4 rad, iteration counts within one."""
+    from distpca_gb300 import synth
+
+    n_ind, nrhs = 806, 8
+    widths = [1300, 3001, 777]
+    c = synth.make_cohort(n_ind, int(sum(widths)), n_pop=3, fst=0.08, missing=0.01, seed=21)
+    packed = synth.pack_rows(c)
+    flags = dict(nsv=2, power=3, crit=1, tol=1e-6, miter=20)
+    with dpca.Windows(n_ind, widths, nrhs) as w:
+        w.upload(packed)
+        r = w.solve(**flags)
+    offs = np.concatenate([[0], np.cumsum(widths)])
+    for i in range(len(widths)):
+        s0, s1 = int(offs[i]), int(offs[i + 1])
+        ref = oracle.solve(packed[s0:s1], n_ind, nrhs=nrhs, bsize=s1 - s0 - 1, **flags)
+        lam, lam_r = r["sigma"][i] ** 2, ref["sigma"] ** 2
+        assert np.max(np.abs(lam - lam_r) / lam_r) < 1e-6, (i, lam, lam_r)
+        assert max_angle(r["u"][i], ref["u"]) < 1e-4, i
+        assert abs(int(r["its"][i]) - ref["its"]) <= 1, (i, r["its"][i], ref["its"])
