@@ -43,6 +43,9 @@ class Config(ctypes.Structure):
 
 
 _D = ctypes.POINTER(ctypes.c_double)
+# dpca_block_fn: int fn(void *ctx, int64_t first_snp, int n_rows, const uint8_t **rows, int64_t *row_stride)
+BLOCK_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64))
 
 
 class Result(ctypes.Structure):
@@ -105,6 +108,9 @@ _SIGS = {
                                             ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "dpca_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dpca_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "dpca_upload_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "dpca_inject_fault": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
+    "dpca_upload_blocks": (ctypes.c_int, [ctypes.c_void_p, BLOCK_FN, ctypes.c_void_p, ctypes.c_int64]),
     "dpca_synth_fill": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_int]),
     "dpca_download_packed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
@@ -338,6 +344,30 @@ class Handle:
 
     def upload_ptr(self, ptr: int, row_stride: int) -> None:
         _check(lib().dpca_upload(self._h, ctypes.c_void_p(ptr), row_stride))
+
+    def inject_fault(self, fault: int = 1, wait_limit_ms: float = 1.0) -> None:
+        """Test hook: the next mixed X Omega launch withholds one load; its bounded wait runs out."""
+        _check(lib().dpca_inject_fault(self._h, fault, wait_limit_ms))
+
+    def upload_file(self, bed_path: str) -> None:
+        """Rows from a SNP-major .bed through the library's block reader (read every pass when
+        streaming)."""
+        _check(lib().dpca_upload_file(self._h, bed_path.encode()))
+
+    def upload_blocks(self, fn, max_row_stride: int) -> None:
+        """Rows handed out by fn(first_snp, n_rows) -> (host address, row stride) per block."""
+
+        def cb(ctx, s0, rows, out_ptr, out_stride):
+            try:
+                ptr, stride = fn(int(s0), int(rows))
+            except Exception:
+                return 1
+            out_ptr[0] = ptr
+            out_stride[0] = stride
+            return 0
+
+        self._blocks_cb = BLOCK_FN(cb)  # kept alive for as long as the handle may call it
+        _check(lib().dpca_upload_blocks(self._h, self._blocks_cb, None, max_row_stride))
 
     def synth_fill(self, cohort) -> None:
         pop = np.ascontiguousarray(cohort.pop, dtype=np.uint8)

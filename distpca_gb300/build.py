@@ -23,7 +23,7 @@ CLI = os.path.join(OUT, "dpca")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["k_stats.cu", "k_fp64.cu", "k_dense.cu", "k_mixed.cu", "k_fullsvd.cu", "k_windows.cu", "handle.cu"]
-CPP_SOURCES = ["host.cpp", "serve.cpp", "eig_host.cpp"]
+CPP_SOURCES = ["host.cpp", "serve.cpp", "eig_host.cpp", "rows.cpp"]
 
 
 def nvcc() -> str:

@@ -6,7 +6,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <condition_variable>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dpca.h"
@@ -63,6 +66,76 @@ struct ScopedLaunch {
     ~ScopedLaunch();
 };
 
+// Where a handle's packed SNP rows come from (rows.cpp): a .bed file read with positional reads,
+// caller rows in host memory, or a caller callback that hands out each block's rows.
+struct RowSource {
+    enum Kind { kNone, kMemory, kBlocks, kFile } kind = kNone;
+    const uint8_t *base = nullptr;  // memory: row r at base + r * stride
+    int64_t stride = 0;
+    bool pinned = false;
+    dpca_block_fn fn = nullptr;     // blocks
+    void *ctx = nullptr;
+    int64_t max_stride = 0;         // blocks: the largest row stride fn returns
+    int fd = -1;                    // file
+    int64_t header = 0;
+    std::string path;
+    int64_t np = 0;                 // bytes per row as stored contiguously in a ring slot = ceil(n_ind / 4)
+    RowSource() = default;
+    RowSource(const RowSource &) = delete;
+    RowSource &operator=(const RowSource &) = delete;
+    ~RowSource();
+    dpca_status open_file(const char *bed_path, int64_t row_bytes);
+    void set_memory(const uint8_t *rows, int64_t row_stride, int64_t row_bytes);
+    void set_blocks(dpca_block_fn f, void *c, int64_t row_bytes, int64_t max_row_stride);
+    // Rows [s0, s0 + rows) in place (memory and blocks sources); *pin says whether the copy
+    // engine can read them directly.
+    dpca_status direct(int64_t s0, int rows, const uint8_t **ptr, int64_t *row_stride, bool *pin) const;
+    // Rows [s0, s0 + rows) copied into dst, np bytes per row (several threads).
+    dpca_status read_into(int64_t s0, int rows, uint8_t *dst, std::string *err) const;
+    // Whether blocks go through the pinned ring (file rows; memory and callback rows are copied in place).
+    bool use_ring = false;
+    // Row stride of what the device receives: np out of the ring, else the source's own stride.
+    int64_t copy_stride() const { return use_ring ? np : kind == kMemory ? stride : max_stride; }
+};
+
+// Pinned host staging slots filled by a reader thread ahead of the device (rows.cpp).
+class HostRing {
+  public:
+    static constexpr int kSlots = 3;
+    ~HostRing();
+    // Begin a sweep over blocks ({first row, rows} each) of src; slots are (re)allocated to fit.
+    dpca_status start(const RowSource *src, std::vector<std::pair<int64_t, int>> blocks);
+    // Wait (bounded) until block i of the sweep sits in a slot; *ptr = its rows, np bytes apart.
+    dpca_status acquire(int i, const uint8_t **ptr);
+    // Block i's copy out of its slot is enqueued on `stream`: the slot is refilled after it.
+    dpca_status release(int i, cudaStream_t stream);
+    size_t slot_size() const { return slot_bytes; }
+
+  private:
+    enum State { kFree, kFilling, kReady, kInUse, kReleased };
+    struct Slot {
+        uint8_t *buf = nullptr;
+        cudaEvent_t done = nullptr;
+        State state = kFree;
+        int block = -1;
+    };
+    dpca_status ensure(size_t bytes);
+    void shutdown();
+    void reader_main();
+    std::mutex mu;
+    std::condition_variable cv;
+    std::thread reader;
+    std::vector<Slot> slots;
+    size_t slot_bytes = 0;
+    bool stop = false;
+    const RowSource *sweep_src = nullptr;
+    std::vector<std::pair<int64_t, int>> sweep;
+    int next_read = 0;
+    uint64_t generation = 0;
+    dpca_status failed = DPCA_OK;
+    std::string fail_msg;
+};
+
 struct Handle {
     int device = 0;
     int sm_count = 0;
@@ -107,8 +180,8 @@ struct Handle {
     bool streamed = false;
     int blk = 0, nblk = 0;            // SNP rows per block (multiple of 128), number of blocks
     int rows_dev = 0;                 // SNP rows resident at a time: n_snp, or blk when streamed
-    const uint8_t *hostP = nullptr;   // caller-owned host rows, host_stride bytes apart
-    int64_t host_stride = 0;
+    RowSource *src = nullptr;         // where the rows come from (set by dpca_upload*, owned)
+    HostRing *ring = nullptr;         // pinned staging for sources the copy engine cannot read in place
     uint8_t *Pb[2] = {nullptr, nullptr};   // block buffers, blk x pitch
     uint8_t *PTb[2] = {nullptr, nullptr};  // mixed: block transposes, pitchTb per individual, tiled as PT
     int64_t pitchTb = 0;
@@ -117,10 +190,15 @@ struct Handle {
                                            // whose stride is not the device pitch), re-pitched on device
     cudaStream_t cstream = nullptr;        // copy stream
     cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+    cudaEvent_t staged_free[2] = {nullptr, nullptr};  // Sb[b] re-pitched (recorded on the compute stream)
 
     // Device allocations: cudaMalloc, or stream-ordered on `stream` (cudaMallocAsync / cudaFreeAsync)
     // for handles of the serving loop, so that creating and freeing one job's buffers never
     // synchronises the device under the other jobs' work.  dev_bytes counts what is held.
+    // Test hook (dpca_inject_fault): a fault for the next mixed X Omega launch and its wait limit.
+    int inject_fault = 0;
+    long long inject_wait_cycles = 0;
+
     bool async_alloc = false;
     cudaMemPool_t pool = nullptr;  // the pool stream-ordered allocations come from (NULL: the device's default)
     size_t dev_bytes = 0;

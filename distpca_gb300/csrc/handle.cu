@@ -182,9 +182,14 @@ static void free_all(Handle *h) {
                     h->small, h->red,   h->dflag,  h->Pb[0],    h->Pb[1], h->PTb[0], h->PTb[1],
                     h->Sb[0], h->Sb[1]};
     for (void *p : ptrs) dev_free(h, p);
+    delete h->ring;  // waits for copies still reading its slots
+    h->ring = nullptr;
+    delete h->src;
+    h->src = nullptr;
     for (int b = 0; b < 2; ++b) {
         if (h->copied[b]) cudaEventDestroy(h->copied[b]);
         if (h->consumed[b]) cudaEventDestroy(h->consumed[b]);
+        if (h->staged_free[b]) cudaEventDestroy(h->staged_free[b]);
     }
     if (h->cstream) cudaStreamDestroy(h->cstream);
     if (h->host_small) {
@@ -259,8 +264,10 @@ static dpca_status create_impl(Handle *h, int n_ind, int n_snp, int nrhs, int pr
             }
             DPCA_CUDA(cudaEventCreateWithFlags(&h->copied[b], cudaEventDisableTiming));
             DPCA_CUDA(cudaEventCreateWithFlags(&h->consumed[b], cudaEventDisableTiming));
+            DPCA_CUDA(cudaEventCreateWithFlags(&h->staged_free[b], cudaEventDisableTiming));
             // the first copy into buffer b (copy stream) waits for its zeroing (compute stream)
             DPCA_CUDA(cudaEventRecord(h->consumed[b], h->stream));
+            DPCA_CUDA(cudaEventRecord(h->staged_free[b], h->stream));
         }
         DPCA_CUDA(cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking));
     } else {
@@ -348,32 +355,89 @@ dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int n
     return DPCA_OK;
 }
 
-// Streaming: copy block j of the host rows into buffer j % 2 on the copy stream, after the
-// compute stream has finished with the block that used that buffer last, and make the compute
-// stream wait for the copy.
+// The blocks of a sweep over the rows: {first SNP, rows} of each block of `rows_per` rows.
+static std::vector<std::pair<int64_t, int>> block_list(int n_snp, int rows_per) {
+    std::vector<std::pair<int64_t, int>> v;
+    for (int64_t s0 = 0; s0 < n_snp; s0 += rows_per) v.push_back({s0, (int)std::min<int64_t>(rows_per, n_snp - s0)});
+    return v;
+}
+
+// Host rows of block i of the current sweep, rows [s0, s0 + ns): in place (pinned memory or
+// callback blocks), or out of the pinned ring (file rows, pageable rows).  *via_ring tells the
+// caller to release the ring slot once the block's copy is enqueued.
+static dpca_status block_rows(Handle *h, int i, int64_t s0, int ns, const uint8_t **ptr, int64_t *stride,
+                              bool *via_ring) {
+    *via_ring = h->src->use_ring;
+    if (*via_ring) {
+        *stride = h->np;
+        return h->ring->acquire(i, ptr);
+    }
+    bool pin = false;
+    return h->src->direct(s0, ns, ptr, stride, &pin);
+}
+
+// Streaming: block j of the rows into buffer j % 2.  The copy stream runs only host-to-device
+// copies, back to back: rows at the device pitch go straight into Pb, others contiguously into
+// the staging buffer Sb, which the compute stream re-pitches into Pb.  The copy into a buffer
+// waits until the compute stream is done with the block that used it before; the compute stream
+// waits for the copy.
 static dpca_status stream_in(Handle *h, int j, int *s0, int *ns) {
     const int b = j & 1;
     *s0 = j * h->blk;
     *ns = std::min(h->blk, h->n_snp - *s0);
-    DPCA_CUDA(cudaStreamWaitEvent(h->cstream, h->consumed[b], 0));
-    const uint8_t *src = h->hostP + (int64_t)*s0 * h->host_stride;
-    if (h->Sb[b]) {
-        // host rows are not at the device pitch: one contiguous copy (full link speed; a
-        // row-pitched host copy ran ~35% slower), then a device-side re-pitch
-        DPCA_CUDA(cudaMemcpyAsync(h->Sb[b], src, (size_t)*ns * h->host_stride, cudaMemcpyHostToDevice, h->cstream));
-        DPCA_CUDA(cudaMemcpy2DAsync(h->Pb[b], h->pitch, h->Sb[b], h->host_stride, h->np, *ns,
-                                    cudaMemcpyDeviceToDevice, h->cstream));
+    const uint8_t *src = nullptr;
+    int64_t stride = 0;
+    bool via_ring = false;
+    DPCA_TRY(block_rows(h, j, *s0, *ns, &src, &stride, &via_ring));
+    const bool staged = stride != h->pitch;
+    cudaStream_t cs = h->cstream;
+    dpca_status st = DPCA_OK;
+    auto check = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == DPCA_OK) {
+            set_error("streamed block %d: %s: %s", j, what, cudaGetErrorString(e));
+            st = DPCA_ERR_CUDA;
+        }
+    };
+    if (staged && (size_t)*ns * stride > h->sb_bytes) {
+        set_error("streamed block %d: rows of stride %lld exceed the staging buffer", j, (long long)stride);
+        st = DPCA_ERR_INVALID;
     } else {
-        DPCA_CUDA(cudaMemcpy2DAsync(h->Pb[b], h->pitch, src, h->host_stride, h->np, *ns, cudaMemcpyHostToDevice,
-                                    h->cstream));
+        check(cudaStreamWaitEvent(cs, staged ? h->staged_free[b] : h->consumed[b], 0), "wait");
+        check(cudaMemcpyAsync(staged ? h->Sb[b] : h->Pb[b], src, (size_t)*ns * stride, cudaMemcpyHostToDevice, cs),
+              "host-to-device copy");
     }
-    DPCA_CUDA(cudaEventRecord(h->copied[b], h->cstream));
+    if (via_ring) {  // always hand the slot back, also after an error
+        dpca_status rs = h->ring->release(j, cs);
+        if (st == DPCA_OK) st = rs;
+    }
+    DPCA_TRY(st);
+    DPCA_CUDA(cudaEventRecord(h->copied[b], cs));
     DPCA_CUDA(cudaStreamWaitEvent(h->stream, h->copied[b], 0));
+    if (staged) {
+        // Pb[b] is free here: the compute stream's own earlier work on it precedes
+        DPCA_CUDA(cudaMemcpy2DAsync(h->Pb[b], h->pitch, h->Sb[b], stride, h->np, *ns, cudaMemcpyDeviceToDevice,
+                                    h->stream));
+        DPCA_CUDA(cudaEventRecord(h->staged_free[b], h->stream));
+    }
     return DPCA_OK;
+}
+
+static dpca_status start_sweep(Handle *h, int rows_per) {
+    if (!h->src || h->src->kind == RowSource::kNone) {
+        set_error("no genotype rows attached (call dpca_upload, dpca_upload_file or dpca_upload_blocks)");
+        return DPCA_ERR_INVALID;
+    }
+    if (!h->src->use_ring) return DPCA_OK;
+    if (!h->ring) {
+        h->ring = new (std::nothrow) HostRing();
+        if (!h->ring) return DPCA_ERR_NOMEM;
+    }
+    return h->ring->start(h->src, block_list(h->n_snp, rows_per));
 }
 
 // Per-SNP statistics of a streamed matrix: one sweep over the blocks.
 static dpca_status streamed_stats(Handle *h) {
+    DPCA_TRY(start_sweep(h, h->blk));
     for (int j = 0; j < h->nblk; ++j) {
         int s0 = 0, ns = 0;
         DPCA_TRY(stream_in(h, j, &s0, &ns));
@@ -393,6 +457,7 @@ static dpca_status streamed_stats(Handle *h) {
 // One pass over a streamed matrix: blocks arrive double-buffered; Z accumulates over them.
 static dpca_status streamed_pass(Handle *h, const double *in, double *out) {
     if (h->precision == DPCA_PREC_MIXED) DPCA_TRY(mixed_omega_operand(h, in));
+    DPCA_TRY(start_sweep(h, h->blk));
     for (int j = 0; j < h->nblk; ++j) {
         int s0 = 0, ns = 0;
         DPCA_TRY(stream_in(h, j, &s0, &ns));
@@ -581,15 +646,16 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     return DPCA_OK;
 }
 
-// Resident upload, pipelined in chunks of whole 512-SNP tiles: each chunk's rows are copied
-// contiguously (full host-link speed; a row-pitched copy of .bed-layout rows ran ~25% slower)
-// into a staging buffer on a copy stream, re-pitched into P on the device, and its per-SNP
-// statistics and transposed tiles computed while the next chunk is copied.
-static dpca_status upload_pipelined(Handle *h, const uint8_t *packed, int64_t row_stride) {
+// Resident upload, pipelined in chunks of whole 512-SNP tiles: each chunk's rows (in place, or out
+// of the pinned ring for file and pageable rows) are copied contiguously (full host-link speed; a
+// row-pitched copy of .bed-layout rows ran ~25% slower) into a staging buffer on a copy stream,
+// re-pitched into P on the device, and its per-SNP statistics and transposed tiles computed while
+// the next chunk is copied.
+static dpca_status upload_pipelined(Handle *h) {
     ScopedLaunch t(&h->clock, h->stream, "h2d_packed");
-    int64_t rows_per = std::max<int64_t>(512, ((int64_t)(256 << 20) / std::max<int64_t>(1, row_stride)) / 512 * 512);
+    const int64_t cstride = h->src->copy_stride();
+    int64_t rows_per = std::max<int64_t>(512, ((int64_t)(256 << 20) / std::max<int64_t>(1, cstride)) / 512 * 512);
     rows_per = std::min<int64_t>(rows_per, ((int64_t)h->n_snp + 511) / 512 * 512);
-    const bool direct = row_stride == h->pitch;  // rows already at the device pitch
     dpca_status st = DPCA_OK;
     auto check = [&](cudaError_t e, const char *what) {
         if (e != cudaSuccess && st == DPCA_OK) {
@@ -600,40 +666,52 @@ static dpca_status upload_pipelined(Handle *h, const uint8_t *packed, int64_t ro
     };
     // copy stream, events and staging buffers are kept by the handle (freed with it)
     if (!h->cstream) check(cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking), "stream");
+    const size_t stage_bytes = (size_t)rows_per * cstride;
     for (int b = 0; b < 2 && st == DPCA_OK; ++b) {
         if (!h->copied[b]) check(cudaEventCreateWithFlags(&h->copied[b], cudaEventDisableTiming), "event");
         if (!h->consumed[b]) check(cudaEventCreateWithFlags(&h->consumed[b], cudaEventDisableTiming), "event");
-        if (!direct && (!h->Sb[b] || h->sb_bytes < (size_t)rows_per * row_stride)) {
+        if (!h->Sb[b] || h->sb_bytes < stage_bytes) {
             dev_free(h, h->Sb[b]);
             h->Sb[b] = nullptr;
-            if (st == DPCA_OK) st = dev_alloc(h, (void **)&h->Sb[b], (size_t)rows_per * row_stride);
+            if (st == DPCA_OK) st = dev_alloc(h, (void **)&h->Sb[b], stage_bytes);
         }
         // the copy stream's first use of each buffer waits for everything queued on the compute
         // stream so far: the allocations (stream-ordered ones are usable from that point) and
         // the zeroing of P
         check(cudaEventRecord(h->consumed[b], h->stream), "record");
     }
-    if (!direct && st == DPCA_OK) h->sb_bytes = (size_t)rows_per * row_stride;
+    if (st == DPCA_OK) h->sb_bytes = std::max(h->sb_bytes, stage_bytes);
+    if (st == DPCA_OK) st = start_sweep(h, (int)rows_per);
     cudaStream_t cs = h->cstream;
-    uint8_t **stage = h->Sb;
-    cudaEvent_t *copied = h->copied, *freed = h->consumed;
     for (int64_t s0 = 0, j = 0; s0 < h->n_snp && st == DPCA_OK; s0 += rows_per, ++j) {
         const int b = (int)(j & 1);
         const int rows = (int)std::min<int64_t>(rows_per, h->n_snp - s0);
-        const uint8_t *src = packed + s0 * row_stride;
+        const uint8_t *src = nullptr;
+        int64_t stride = 0;
+        bool via_ring = false;
+        st = block_rows(h, (int)j, s0, rows, &src, &stride, &via_ring);
+        if (st != DPCA_OK) break;
         uint8_t *dst = h->P + s0 * h->pitch;
-        check(cudaStreamWaitEvent(cs, freed[b], 0), "wait");
-        if (direct)
-            check(cudaMemcpyAsync(dst, src, (size_t)rows * row_stride, cudaMemcpyHostToDevice, cs), "copy");
-        else
-            check(cudaMemcpyAsync(stage[b], src, (size_t)rows * row_stride, cudaMemcpyHostToDevice, cs), "copy");
-        check(cudaEventRecord(copied[b], cs), "record");
-        check(cudaStreamWaitEvent(h->stream, copied[b], 0), "wait");
+        const bool direct = stride == h->pitch;  // rows already at the device pitch
+        if ((size_t)rows * stride > h->sb_bytes && !direct) {
+            set_error("upload: rows of stride %lld exceed the staging buffer", (long long)stride);
+            st = DPCA_ERR_INVALID;
+        }
+        check(cudaStreamWaitEvent(cs, h->consumed[b], 0), "wait");
+        check(cudaMemcpyAsync(direct ? (void *)dst : (void *)h->Sb[b], src, (size_t)rows * stride,
+                              cudaMemcpyHostToDevice, cs),
+              "copy");
+        if (via_ring) {
+            dpca_status rs = h->ring->release((int)j, cs);
+            if (st == DPCA_OK) st = rs;
+        }
+        check(cudaEventRecord(h->copied[b], cs), "record");
+        check(cudaStreamWaitEvent(h->stream, h->copied[b], 0), "wait");
         if (!direct)
-            check(cudaMemcpy2DAsync(dst, h->pitch, stage[b], row_stride, h->np, rows, cudaMemcpyDeviceToDevice,
-                                    h->stream),
+            check(cudaMemcpy2DAsync(dst, h->pitch, h->Sb[b], stride, h->np, rows, cudaMemcpyDeviceToDevice, h->stream),
                   "re-pitch");
-        check(cudaEventRecord(freed[b], h->stream), "record");
+        check(cudaEventRecord(h->consumed[b], h->stream), "record");
+        if (st != DPCA_OK) break;
         launch_snp_stats_raw(dst, h->pitch, h->n_ind, rows, h->inv_sqrt_nsnp, h->counts + 4 * s0, h->avg + s0,
                              h->sd + s0, h->lut + 4 * s0, h->coef + 2 * s0, h->stream);
         if (h->precision == DPCA_PREC_MIXED)
@@ -641,6 +719,35 @@ static dpca_status upload_pipelined(Handle *h, const uint8_t *packed, int64_t ro
         check(cudaGetLastError(), "launch");
     }
     return st;
+}
+
+// Attach a row source to the handle (replacing any earlier one) and load it: a resident handle
+// copies every row to the device now; a streaming handle computes its per-SNP statistics in one
+// sweep and reads the rows again in every pass.
+static dpca_status attach_source(Handle *h, RowSource *src) {
+    if (h->ring) {
+        delete h->ring;  // its reader may hold the old source
+        h->ring = nullptr;
+    }
+    delete h->src;
+    h->src = src;
+    h->stats_ready = false;
+    if (h->streamed) {
+        const int64_t cs = src->copy_stride();
+        if (cs != h->pitch) {
+            for (int b = 0; b < 2; ++b) {
+                dev_free(h, h->Sb[b]);  // the compute stream is ordered after every copy that used it
+                h->Sb[b] = nullptr;
+                DPCA_TRY(dev_alloc(h, (void **)&h->Sb[b], (size_t)h->blk * cs));
+                DPCA_CUDA(cudaEventRecord(h->staged_free[b], h->stream));
+            }
+            h->sb_bytes = (size_t)h->blk * cs;
+        }
+        return after_data(h);
+    }
+    DPCA_TRY(upload_pipelined(h));
+    h->stats_ready = true;
+    return DPCA_OK;
 }
 
 }  // namespace dpca
@@ -704,27 +811,41 @@ dpca_status dpca_upload(dpca_handle *hh, const uint8_t *packed, int64_t row_stri
         return DPCA_ERR_INVALID;
     }
     DPCA_CUDA(cudaSetDevice(h->device));
-    if (h->streamed) {
-        // the rows stay in host memory and are read block by block in every pass
-        h->hostP = packed;
-        h->host_stride = row_stride;
-        if (row_stride != h->pitch) {
-            for (int b = 0; b < 2; ++b) {
-                dev_free(h, h->Sb[b]);  // the compute stream is ordered after every copy that used it
-                h->Sb[b] = nullptr;
-                DPCA_TRY(dalloc(h, &h->Sb[b], (size_t)h->blk * row_stride));
-                h->sb_bytes = (size_t)h->blk * row_stride;
-                DPCA_CUDA(cudaEventRecord(h->consumed[b], h->stream));
-            }
-        }
-        DPCA_TRY(after_data(h));
-        return DPCA_OK;
-    }
-    DPCA_TRY(upload_pipelined(h, packed, row_stride));
-    h->stats_ready = true;
-    return DPCA_OK;
+    RowSource *src = new (std::nothrow) RowSource();
+    if (!src) return DPCA_ERR_NOMEM;
+    src->set_memory(packed, row_stride, h->np);
+    return attach_source(h, src);
 }
 
+dpca_status dpca_upload_file(dpca_handle *hh, const char *bed_path) {
+    clear_error();
+    if (!hh || !bed_path) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    DPCA_CUDA(cudaSetDevice(h->device));
+    RowSource *src = new (std::nothrow) RowSource();
+    if (!src) return DPCA_ERR_NOMEM;
+    dpca_status st = src->open_file(bed_path, h->np);
+    if (st != DPCA_OK) {
+        delete src;
+        return st;
+    }
+    return attach_source(h, src);
+}
+
+dpca_status dpca_upload_blocks(dpca_handle *hh, dpca_block_fn fn, void *ctx, int64_t max_row_stride) {
+    clear_error();
+    if (!hh || !fn) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    if (max_row_stride < h->np) {
+        set_error("max_row_stride %lld < ceil(n_ind/4) = %lld", (long long)max_row_stride, (long long)h->np);
+        return DPCA_ERR_INVALID;
+    }
+    DPCA_CUDA(cudaSetDevice(h->device));
+    RowSource *src = new (std::nothrow) RowSource();
+    if (!src) return DPCA_ERR_NOMEM;
+    src->set_blocks(fn, ctx, h->np, max_row_stride);
+    return attach_source(h, src);
+}
 
 dpca_status dpca_synth_fill(dpca_handle *hh, uint64_t key, const uint8_t *pop, const uint32_t *miss_thr,
                             const uint32_t *snp_thr, int n_pop) {
@@ -772,12 +893,14 @@ dpca_status dpca_download_packed(dpca_handle *hh, int s0, int s1, uint8_t *out) 
     }
     DPCA_CUDA(cudaSetDevice(h->device));
     if (h->streamed) {
-        if (!h->hostP) {
-            set_error("no genotype rows attached (call dpca_upload)");
+        if (!h->src || h->src->kind == RowSource::kNone) {
+            set_error("no genotype rows attached (call dpca_upload, dpca_upload_file or dpca_upload_blocks)");
             return DPCA_ERR_INVALID;
         }
-        for (int s = s0; s < s1; ++s) memcpy(out + (size_t)(s - s0) * h->np, h->hostP + (int64_t)s * h->host_stride, h->np);
-        return DPCA_OK;
+        std::string err;
+        dpca_status st = s1 > s0 ? h->src->read_into(s0, s1 - s0, out, &err) : DPCA_OK;
+        if (st != DPCA_OK) set_error("%s", err.c_str());
+        return st;
     }
     if (s1 > s0)
         DPCA_CUDA(cudaMemcpy2DAsync(out, h->np, h->P + (int64_t)s0 * h->pitch, h->pitch, h->np, s1 - s0,
@@ -873,6 +996,25 @@ dpca_status dpca_reset_kernel_times(dpca_handle *hh, int enable) {
     if (!hh) return DPCA_ERR_INVALID;
     hh->h.clock.reset();
     hh->h.clock.enabled = enable != 0;
+    return DPCA_OK;
+}
+
+dpca_status dpca_inject_fault(dpca_handle *hh, int fault, double wait_limit_ms) {
+    clear_error();
+    if (!hh || fault < 0 || fault > 1 || !(wait_limit_ms > 0.0) || wait_limit_ms > 10000.0) {
+        set_error("dpca_inject_fault: fault must be 0 or 1 and the wait limit in (0, 10000] ms");
+        return DPCA_ERR_INVALID;
+    }
+    Handle *h = &hh->h;
+    if (h->precision != DPCA_PREC_MIXED) {
+        set_error("dpca_inject_fault: the fault is in the mixed-precision product kernel");
+        return DPCA_ERR_UNSUPPORTED;
+    }
+    int clock_khz = 0;
+    DPCA_CUDA(cudaDeviceGetAttribute(&clock_khz, cudaDevAttrClockRate, h->device));
+    h->inject_fault = fault;
+    // cycles at the highest SM clock: the wait lasts at least the requested time
+    h->inject_wait_cycles = (long long)(wait_limit_ms * (double)std::max(clock_khz, 1000));
     return DPCA_OK;
 }
 

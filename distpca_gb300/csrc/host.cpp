@@ -79,22 +79,6 @@ static int ram_kb() {
     return kb;
 }
 
-// Positional read of [off, off+len) into buf, looping over short reads.
-static dpca_status pread_all(int fd, uint8_t *buf, size_t len, off_t off, const char *path) {
-    while (len > 0) {
-        ssize_t got = pread(fd, buf, len, off);
-        if (got < 0 && errno == EINTR) continue;
-        if (got <= 0) {
-            set_error("short read of %s at offset %lld", path, (long long)off);
-            return DPCA_ERR_IO;
-        }
-        buf += got;
-        off += got;
-        len -= (size_t)got;
-    }
-    return DPCA_OK;
-}
-
 static std::string construct_filename(const std::string &pure, const char *type) {
     time_t raw;
     time(&raw);
@@ -196,42 +180,20 @@ static dpca_status run_common(const dpca_config *cfg_in, const char *bfile, cons
         DPCA_TRY(dpca_create_streamed(&hh, n_ind, n_snp, cfg.nrhs, cfg.precision, cfg.device, nullptr, block_snps));
     else
         DPCA_TRY(dpca_create(&hh, n_ind, n_snp, cfg.nrhs, cfg.precision, cfg.device, nullptr));
-    std::vector<uint8_t> filebuf;
-    uint8_t *pinned = nullptr;
-    const uint8_t *src = packed_host;
-    int64_t stride = row_stride;
     dpca_status st = DPCA_OK;
-    if (!src) {
-        // the whole .bed payload, in pinned memory when the host allows it
+    if (packed_host) {
+        st = dpca_upload(hh, packed_host, row_stride);
+    } else {
+        // the .bed rows through the handle's block reader: read once for a resident matrix, every
+        // pass for a streamed one -- never the whole file in host memory at once
         std::string bed = std::string(bfile) + ".bed";
-        int fd = open(bed.c_str(), O_RDONLY);
-        if (fd < 0) {
-            dpca_destroy(hh);
-            set_error("[Data::read_bed] Error reading file %s", bed.c_str());
-            return DPCA_ERR_IO;
-        }
-        size_t bytes = (size_t)np * n_snp;
-        uint8_t *buf = nullptr;
-        if (cudaMallocHost((void **)&pinned, std::max<size_t>(bytes, 1)) == cudaSuccess) {
-            buf = pinned;
-        } else {
-            cudaGetLastError();
-            pinned = nullptr;
-            filebuf.resize(bytes);
-            buf = filebuf.data();
-        }
-        st = pread_all(fd, buf, bytes, 3, bed.c_str());
-        close(fd);
-        src = buf;
-        stride = np;
+        st = dpca_upload_file(hh, bed.c_str());
     }
-    if (st == DPCA_OK) st = dpca_upload(hh, src, stride);
     if (st == DPCA_OK) st = dpca_synchronize(hh);
     double t1 = wall_now();
     res->time_load_matrix = t1 - t0;
     if (st == DPCA_OK) st = dpca_solve(hh, &cfg, omega_inout, res);
     dpca_destroy(hh);
-    if (pinned) cudaFreeHost(pinned);
     res->time_total = wall_now() - t0 + res->time_generate_rhs;
     return st;
 }
@@ -517,27 +479,10 @@ dpca_status dpca_full_svd(const dpca_config *cfg, const char *bfile, const uint8
         set_error("-fullSVD: nsv %d outside [1, min(n_ind, n_snp)]", nsv);
         return DPCA_ERR_INVALID;
     }
-    const int64_t np = (n_ind + 3) / 4;
-    std::vector<uint8_t> filebuf;
-    const uint8_t *src = packed;
-    int64_t stride = row_stride;
-    if (!src) {
-        std::string bed = std::string(bfile) + ".bed";
-        int fd = open(bed.c_str(), O_RDONLY);
-        if (fd < 0) {
-            set_error("[Data::read_bed] Error reading file %s", bed.c_str());
-            return DPCA_ERR_IO;
-        }
-        filebuf.resize((size_t)np * n_snp);
-        dpca_status st = pread_all(fd, filebuf.data(), filebuf.size(), 3, bed.c_str());
-        close(fd);
-        DPCA_TRY(st);
-        src = filebuf.data();
-        stride = np;
-    }
     dpca_handle *hh = nullptr;
     DPCA_TRY(dpca_create(&hh, n_ind, n_snp, 128, DPCA_PREC_FP64, cfg->device, nullptr));
-    dpca_status st = dpca_upload(hh, src, stride);
+    dpca_status st = packed ? dpca_upload(hh, packed, row_stride)
+                            : dpca_upload_file(hh, (std::string(bfile) + ".bed").c_str());
     std::vector<double> tu((size_t)n_ind * nsv);
     const double t0 = wall_now();
     if (st == DPCA_OK) st = full_svd_device(&hh->h, nsv, out->true_sigma, tu.data(), &out->info);

@@ -109,7 +109,16 @@ struct GemmArgs {
     const int *win_kb0, *win_nkb;
     const int *win_active;
     int tiles, items;  // work items = tiles x splits (tile fastest); the grid is one CTA per SM at most
+    // Limit of every barrier wait, in cycles (normally ~4 s).  A test shortens it together with
+    // `inject` = 1, which makes CTA 0's load producer withhold its first batch: the MMA issuer's
+    // wait for that batch then runs out, the kernel reports DPCA_ERR_TIMEOUT and exits cleanly.
+    long long wait_cycles = tc::kWaitCycles;
+    int inject = 0;
 };
+
+// How long a role waits, on the way out after an error, for asynchronous work it started (TMA
+// copies, MMAs) to finish: far longer than either takes.
+constexpr long long kExitCycles = 4000000;
 
 struct MixedState {
     int kp = 0, N = 0;
@@ -241,12 +250,12 @@ __device__ __forceinline__ DF df_mul_int(DF c, long long x) {
 
 // Slow path of a wait, out of line so that the MMA issue loop stays compact (an inlined wait
 // loop in that loop costs ~90 cycles per iteration even when it never runs).
-__device__ __noinline__ bool wait_slow(uint64_t *bar, uint32_t parity, int *err, int code) {
-    return tc::mbar_wait(bar, parity, err, code);
+__device__ __noinline__ bool wait_slow(uint64_t *bar, uint32_t parity, int *err, int code, long long limit) {
+    return tc::mbar_wait(bar, parity, err, code, false, limit);
 }
 
-__device__ __forceinline__ bool wait_fast(uint64_t *bar, uint32_t parity, int *err, int code) {
-    return tc::mbar_try_wait(bar, parity) || wait_slow(bar, parity, err, code);
+__device__ __forceinline__ bool wait_fast(uint64_t *bar, uint32_t parity, int *err, int code, long long limit) {
+    return tc::mbar_try_wait(bar, parity) || wait_slow(bar, parity, err, code, limit);
 }
 
 // Chunks of an accumulator whose first chunk has `first` batches and the others `len`.
@@ -297,7 +306,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t *pk_full = bars, *pk_empty = bars + kPStages;
     uint64_t *full = pk_empty + kPStages, *free_ = full + R;
     uint64_t *acc_full = free_ + R, *acc_empty = acc_full + 2;
-    uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
+    uint64_t *mma_done = acc_empty + 2;  // one per issuer: its MMAs have all completed (kernel exit)
+    uint32_t *tmem_slot = (uint32_t *)(mma_done + 2);
     // X Omega column maxima of this CTA's tiles (one global atomic per column per CTA at the end;
     // per-warp global atomics on the same k addresses from every CTA stalled short-K tiles)
     unsigned int *cmax_s = tmem_slot + 1;
@@ -317,6 +327,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int v = 0; v < 2; ++v) {
             tc::mbar_init(&acc_full[v], 1);
             tc::mbar_init(&acc_empty[v], 4);
+            tc::mbar_init(&mma_done[v], 1);
         }
         tc::fence_mbar_init();
         for (int c = 0; c < kMaxMixedNrhs; ++c) cmax_s[c] = 0u;
@@ -344,12 +355,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             int sp = 0, r = 0, issued_p = 0, issued_b = 0;
             uint32_t pph = 0, bph = 0;
             bool ok = true;
+            bool withhold = args.inject == 1 && blockIdx.x == 0;
+            const long long lim = args.wait_cycles;
             for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
                 const WorkItem x = work_item(args, it);
                 const int b_row0 = args.tile_win ? x.win * N : 0;  // this window's Omega slices
                 for (int t = 0; t < x.nb; ++t) {
                     if ((t & 3) == 0) {
-                        if (!(ok = tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true))) break;
+                        if (!(ok = tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true, lim))) break;
                         tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
                         if (MODE == kXTY)  // tile-blocked: (row block, K tile) at row ((rb * nkt) + kt) * 128
                             tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], 0,
@@ -360,18 +373,31 @@ __global__ void __launch_bounds__(kThreads, 1)
                         ++issued_p;
                         if (++sp == kPStages) sp = 0, pph ^= 1;
                     }
-                    if (!(ok = tc::mbar_wait(&free_[r], bph ^ 1, err, 12, true))) break;
-                    tc::mbar_arrive_expect_tx(&full[r], bstage);
-                    tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, b_row0, x.kb0 + 2 * t);
-                    ++issued_b;
+                    if (!(ok = tc::mbar_wait(&free_[r], bph ^ 1, err, 12, true, lim))) break;
+                    if (withhold) {
+                        withhold = false;  // injected fault: this batch never arrives
+                    } else {
+                        tc::mbar_arrive_expect_tx(&full[r], bstage);
+                        tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, b_row0, x.kb0 + 2 * t);
+                        ++issued_b;
+                    }
                     if (++r == R) r = 0, bph ^= 1;
                 }
             }
-            // drain: every issued copy must land before the CTA may exit
+            // drain: every issued copy must land before the CTA may exit.  After an error the
+            // phases may never complete (their other arrivals gave up), so each wait then falls
+            // back to a bounded wait long enough for any copy in flight to land.
             for (int g = max(0, issued_p - kPStages); g < issued_p; ++g)
-                tc::mbar_wait(&pk_full[g % kPStages], (g / kPStages) & 1, err, 13, true);
-            for (int t = max(0, issued_b - R); t < issued_b; ++t)
-                tc::mbar_wait(&full[t % R], (t / R) & 1, err, 14, true);
+                if (!tc::mbar_wait(&pk_full[g % kPStages], (g / kPStages) & 1, err, 13, true, lim))
+                    tc::mbar_wait_exit(&pk_full[g % kPStages], (g / kPStages) & 1, kExitCycles);
+            if (issued_b > 0) {
+                // batches are numbered by ring position; a withheld batch leaves a gap, so wait on
+                // the phases of the last min(R, issued) ring positions the producer reached
+                const int reached = issued_b + (args.inject == 1 && blockIdx.x == 0 ? 1 : 0);
+                for (int t = max(0, reached - R); t < reached; ++t)
+                    if (!tc::mbar_wait(&full[t % R], (t / R) & 1, err, 14, true, lim))
+                        tc::mbar_wait_exit(&full[t % R], (t / R) & 1, kExitCycles);
+            }
         }
     } else if (warp == 1 || warp == kIssuerWarpM) {
         // ---------------------------------------------------------- MMA issuers
@@ -396,9 +422,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             int left = first_len;
             bool fresh = true;
             for (int t = 0; t < nb; ++t) {
-                if (!(ok = __all_sync(0xffffffffu, wait_fast(&full[r], ph, err, 21)))) break;
+                if (!(ok = __all_sync(0xffffffffu, wait_fast(&full[r], ph, err, 21, args.wait_cycles)))) break;
                 if (fresh && cv > 0 &&
-                    !(ok = __all_sync(0xffffffffu, wait_fast(&acc_empty[v], (cv - 1) & 1, err, 22))))
+                    !(ok = __all_sync(0xffffffffu,
+                                      wait_fast(&acc_empty[v], (cv - 1) & 1, err, 22, args.wait_cycles))))
                     break;
                 const bool chunk_done = --left == 0 || t == nb - 1;
                 tc::fence_after_sync();
@@ -427,6 +454,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                 stage ^= 1u;
             }
         }
+        // every MMA this warp issued must have finished before the CTA frees tensor memory, also
+        // after an error: one more commit, whose arrival follows them all
+        if (tc::elect_one_sync()) tc::mma_commit(&mma_done[v]);
+        __syncwarp();
+        tc::mbar_wait_exit(&mma_done[v], 0, kExitCycles);
     } else if (warp >= 2 && warp < 2 + 4 * kDecodeGroups) {
         // ---------------------------------------------------------- decode (warps 2..9)
         // Group grp decodes the batches of odd/even global index (its A stage).  Every group
@@ -447,12 +479,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int nst = (nb + 3) >> 2;
             for (int pgi = 0; ok && pgi < nst; ++pgi) {
                 const int pg = pgl + pgi, sp = pg % kPStages;
-                ok = __all_sync(0xffffffffu, tc::mbar_wait(&pk_full[sp], (pg / kPStages) & 1, err, 31));
+                ok = __all_sync(0xffffffffu,
+                                tc::mbar_wait(&pk_full[sp], (pg / kPStages) & 1, err, 31, false, args.wait_cycles));
                 if (!ok) break;
                 const int t_end = min(4 * pgi + 4, nb);
                 for (int t = 4 * pgi + (((gb + 4 * pgi) & 1) != grp ? 1 : 0); t < t_end; t += 2) {
                     if (gb + t >= 2) {  // this group's A stage was last read by global batch gb + t - 2
-                        ok = __all_sync(0xffffffffu, tc::mbar_wait(&free_[fi], fph, err, 32));
+                        ok = __all_sync(0xffffffffu, tc::mbar_wait(&free_[fi], fph, err, 32, false, args.wait_cycles));
                         fi += 2;
                         if (fi >= R) fi -= R, fph ^= 1;
                         if (!ok) break;
@@ -512,7 +545,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (g_next) ++cG;
                 else ++cM;
                 const int cglob = g_next ? cgG++ : cgM++;
-                ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[v], cglob & 1, err, 41, true));
+                ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[v], cglob & 1, err, 41, true, args.wait_cycles));
                 if (!ok) break;
                 tc::fence_after_sync();
                 // copy the accumulator out (h slices, then l slices), then release it at once
@@ -1060,6 +1093,11 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     a.colsumq = m->colsumq;
     a.y_out = y_out;
     a.err = h->dflag;
+    if (h->inject_fault) {  // test hook: one launch only
+        a.inject = h->inject_fault;
+        a.wait_cycles = h->inject_wait_cycles;
+        h->inject_fault = 0;
+    }
     DPCA_CUDA(cudaMemsetAsync(m->colmax, 0, (size_t)k * 4, h->stream));
     DPCA_CUDA(cudaMemsetAsync(m->rq, 0, (size_t)k * 8, h->stream));
     {

@@ -7,8 +7,8 @@
 //   - file:   pread of the block's byte range from the .bed into a ring slot, by a reader thread
 //             (split over several threads: one thread's pread from the page cache runs at memory-
 //             copy speed, a few GB/s, below the host link);
-//   - memory: caller rows in host memory -- used in place when pinned (the copy engine reads
-//             them directly), copied into a ring slot when pageable;
+//   - memory: caller rows in host memory, copied to the device in place (at full speed when
+//             pinned; pageable rows take the driver's own staging);
 //   - blocks: a caller callback that returns the host address of each block's rows (a
 //             decompressor, a network receiver, a synthetic generator), treated like memory.
 // The ring has kSlots slots of one block each.  Block i of a sweep goes to slot i % kSlots; the
@@ -72,6 +72,7 @@ dpca_status RowSource::open_file(const char *bed_path, int64_t row_bytes) {
     path = bed_path;
     np = row_bytes;
     header = 3;
+    use_ring = true;
     fd = open(bed_path, O_RDONLY);
     if (fd < 0) {
         set_error("[Data::read_bed] Error reading file %s", bed_path);
@@ -87,19 +88,22 @@ dpca_status RowSource::open_file(const char *bed_path, int64_t row_bytes) {
     return DPCA_OK;
 }
 
-void RowSource::set_memory(const uint8_t *rows, int64_t row_stride) {
+void RowSource::set_memory(const uint8_t *rows, int64_t row_stride, int64_t row_bytes) {
     kind = kMemory;
     base = rows;
     stride = row_stride;
-    np = row_stride;
+    np = row_bytes;
     pinned = is_pinned(rows);
+    use_ring = false;
 }
 
-void RowSource::set_blocks(dpca_block_fn f, void *c, int64_t row_bytes) {
+void RowSource::set_blocks(dpca_block_fn f, void *c, int64_t row_bytes, int64_t max_row_stride) {
     kind = kBlocks;
     fn = f;
     ctx = c;
     np = row_bytes;
+    max_stride = max_row_stride;
+    use_ring = false;
 }
 
 // Rows [s0, s0 + rows) in place, when the source can hand them out without a copy.
@@ -115,7 +119,7 @@ dpca_status RowSource::direct(int64_t s0, int rows, const uint8_t **ptr, int64_t
         const uint8_t *p = nullptr;
         int64_t st = 0;
         int rc = fn(ctx, s0, rows, &p, &st);
-        if (rc != 0 || !p || st < np) {
+        if (rc != 0 || !p || st < np || st > max_stride) {
             set_error("block source failed for rows [%lld, %lld) (status %d)", (long long)s0, (long long)s0 + rows, rc);
             return DPCA_ERR_IO;
         }

@@ -63,7 +63,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // clock and the (global) error flag are read only every 256 polls so that the poll loop itself
 // stays off the handoff's critical path; `relaxed` waiters (roles with slack) back off with
 // nanosleep to leave issue slots to the latency-critical warps.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code, bool relaxed = false) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code, bool relaxed = false,
+                                          long long limit = kWaitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     for (uint32_t it = 1;; ++it) {
@@ -71,12 +72,24 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
         if (relaxed && it > 16) __nanosleep(64);
         if ((it & 255u) == 0) {
             if (*(volatile int *)err) return false;
-            if (clock64() - t0 > kWaitCycles) {
+            if (clock64() - t0 > limit) {
                 atomicCAS(err, 0, code);
                 return false;
             }
         }
     }
+}
+
+// Wait for a phase on the way out of a kernel, also after an error: asynchronous work this
+// thread started (TMA copies into shared memory, MMAs reading tensor memory) must be finished
+// before the CTA releases its memory.  Gives up only after `limit` cycles, which such work never
+// takes (a copy of a few KB or a few MMAs): a barrier whose phase also counts arrivals of roles
+// that have already given up never completes, and the limit then bounds the wait.
+__device__ __forceinline__ bool mbar_wait_exit(uint64_t *bar, uint32_t parity, long long limit) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > limit) return false;
+    return true;
 }
 
 // try_wait with a suspend-time hint: the thread sleeps in hardware until the phase completes

@@ -174,6 +174,23 @@ dpca_status dpca_create_streamed(dpca_handle **h, int n_ind, int n_snp, int nrhs
 dpca_status dpca_destroy(dpca_handle *h);
 /* Copy packed rows (host, pinned or pageable) to the device and compute per-SNP statistics. */
 dpca_status dpca_upload(dpca_handle *h, const uint8_t *packed, int64_t row_stride);
+/* The rows of <bed_path> (a SNP-major .bed; its magic is checked), read with positional reads of
+ * whole SNP blocks at 3 + ceil(n_ind/4) * first_snp (the block reader of src/methods.cpp:795-811,
+ * 873-874), through a ring of three pinned staging blocks that a reader thread fills ahead of the
+ * device.  A resident handle reads the file once; a streaming handle reads every block from the
+ * file in every pass and never holds the whole matrix in host memory.  A read that comes up short
+ * returns DPCA_ERR_IO. */
+dpca_status dpca_upload_file(dpca_handle *h, const char *bed_path);
+/* Rows handed out block by block by a caller callback (a decompressor, a network receiver, a
+ * synthetic generator): fn(ctx, first_snp, n_rows, &rows, &row_stride) stores the host address of
+ * SNP rows [first_snp, first_snp + n_rows) and their stride (>= ceil(n_ind/4), <= max_row_stride)
+ * and returns 0 (non-zero: the call that needed the rows fails with DPCA_ERR_IO).  The rows are
+ * copied to the device in place (at full speed when pinned) by stream-ordered copies, so they must
+ * stay valid and unchanged until the work that reads them has finished (dpca_synchronize,
+ * dpca_get_z, or the return of dpca_solve).  A streaming handle calls fn for every block of every
+ * pass; a resident handle once per 256 MB chunk. */
+typedef int (*dpca_block_fn)(void *ctx, int64_t first_snp, int n_rows, const uint8_t **rows, int64_t *row_stride);
+dpca_status dpca_upload_blocks(dpca_handle *h, dpca_block_fn fn, void *ctx, int64_t max_row_stride);
 /* Fill the device matrix with a seeded Balding-Nichols cohort (tables as in distpca_gb300/synth.py):
  * pop[n_ind] uint8, miss_thr[n_ind] uint32, snp_thr[n_snp * n_pop] uint32 (host arrays). */
 dpca_status dpca_synth_fill(dpca_handle *h, uint64_t key, const uint8_t *pop, const uint32_t *miss_thr,
@@ -195,6 +212,16 @@ dpca_status dpca_synchronize(dpca_handle *h);
 dpca_status dpca_kernel_times(dpca_handle *h, char *names, size_t names_cap, double *ms, int64_t *launches,
                               int *count, int cap);
 dpca_status dpca_reset_kernel_times(dpca_handle *h, int enable);
+
+/* ---- test hook: device-side failure detection without a GPU fault ----
+ * Every barrier wait in the product kernels is bounded; when one runs out the kernel records the
+ * site in a device flag, waits (bounded) for its own copies and MMAs in flight, frees its tensor
+ * memory and returns, and the next call that reads results reports DPCA_ERR_TIMEOUT with the
+ * handle still usable.  fault = 1 makes the next mixed X Omega launch of this handle withhold one
+ * load (its first CTA's first batch never arrives), so that the MMA issuer's wait for it runs out
+ * after wait_limit_ms (the normal limit is ~4 s); the setting applies to that one launch.
+ * fault = 0 clears it.  A mixed-precision handle only (DPCA_ERR_UNSUPPORTED otherwise). */
+dpca_status dpca_inject_fault(dpca_handle *h, int fault, double wait_limit_ms);
 
 /* ---- unit-parity entry: decode + counts for packed rows in host memory, on the calling
  * thread's current CUDA device ---- */
