@@ -58,6 +58,12 @@ def parse():
     p.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (jobs/s)")
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-sample", type=int, default=8, help="jobs in the one-at-a-time FP64 comparison")
+    p.add_argument("--serve-stable-jobs", type=int, default=256,
+                   help="jobs in the second stream, offered at 80%% of the capacity the first one measured")
+    p.add_argument("--no-full", action="store_true", help="skip the whole-PCA legs (config 1, converged config 2)")
+    p.add_argument("--no-ooc", action="store_true", help="skip the 500,000-individual out-of-core stream")
+    p.add_argument("--ooc-snps", type=int, default=2_000_000, help="SNPs of the out-of-core stream")
+    p.add_argument("--ooc-distinct", type=int, default=4, help="distinct 2 GB blocks cycled by the out-of-core source")
     return p.parse_args()
 
 
@@ -306,27 +312,37 @@ def dpca_arm(a, ranks: Ranks) -> None:
             "config": workload_config(a), "clocks": clk, "gpu_launches": launches, "roofline": roof, "decode": decode,
             "kernels": kernels}
     # ---- extras (rank 0, untimed): FP64 GPU comparison, accuracy, e2e, CPU baseline ----
-    host = None
+    host = hv = None
     np_bytes = (a.n_ind + 3) // 4
-    if ranks.rank == 0 and not (a.no_e2e and a.no_cpu and a.no_extras):
+    if ranks.rank == 0 and not (a.no_e2e and a.no_extras and a.no_full):
         host = torch.empty((a.n_snp, np_bytes), dtype=torch.uint8, pin_memory=True)
         hv = host.numpy()
         D.lib().dpca_download_packed(h._h, 0, a.n_snp, hv.ctypes.data)
     h.close()
     torch.cuda.empty_cache()
-    if ranks.rank == 0 and not a.no_extras and a.precision == "mixed":
+    if hv is not None and not a.no_extras and a.precision == "mixed":
         line["fp64_gpu"] = fp64_comparison(a, hv, value / ranks.world)
         line["accuracy"] = accuracy_check(a, hv)
-    if ranks.rank == 0 and not a.no_e2e:
+    if hv is not None and not a.no_e2e:
         line["e2e"] = e2e_run(a, hv)
-    if ranks.rank == 0 and not a.no_extras:
+    if hv is not None and not a.no_full and a.precision == "mixed":
+        line["full_pca"] = {"incore50k_converged": converged_run(a, hv)}
+    if hv is not None and not a.no_extras:
         line["streamed"] = streamed_run(a, hv)
+    del hv, host
+    if ranks.rank == 0 and not a.no_full and a.precision == "mixed":
+        line.setdefault("full_pca", {})["config1_1k_x_100k"] = config1_run(a)
+    if ranks.rank == 0 and not a.no_ooc and a.precision == "mixed":
+        line["out_of_core"] = out_of_core_run(a)
     if ranks.rank == 0 and not a.no_windows:
         line["windows"] = windows_run(a)
     if ranks.rank == 0 and not a.no_serve:
-        line["serve"] = serve_run(a)
+        sat = serve_run(a, a.serve_rate, a.serve_jobs, compare=True)
+        stable_rate = round(0.8 * sat["jobs_per_s"], 1)
+        sat["stable_load"] = serve_run(a, stable_rate, a.serve_stable_jobs, compare=False)
+        line["serve"] = sat
     if ranks.rank == 0 and not a.no_cpu and ranks.world == 1:
-        line["cpu_baseline"] = cpu_baseline(a, hv)
+        line["cpu_baseline"] = cpu_baseline_rows(a)
     if ranks.rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -407,21 +423,24 @@ def e2e_run(a, hv) -> dict:
                     "measured just before (the host link is shared on this machine and varies between runs)"}
 
 
-def host_link_gbs(hv) -> float:
-    """Pinned host-to-device bandwidth of a plain 2 GB copy from the bench's host buffer."""
+def host_link_gbs(hv, nbytes: int = 2_000_000_000) -> float:
+    """Host-to-device bandwidth of plain copies (cudaMemcpyAsync, through torch) of the first
+    `nbytes` of the bench's own pinned host buffer -- the memory the timed copies read."""
     import torch
 
-    nbytes = min(hv.nbytes, 2_000_000_000)
+    nbytes = min(hv.nbytes, nbytes)
     src = torch.from_numpy(hv.reshape(-1)[:nbytes])
     dst = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
-    dst.copy_(src, non_blocking=True)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(3):
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
         dst.copy_(src, non_blocking=True)
-    e1.record()
-    torch.cuda.synchronize()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        e1.record(stream)
+    stream.synchronize()
     del dst
     torch.cuda.empty_cache()
     return 3 * nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9
@@ -439,6 +458,7 @@ def streamed_run(a, hv) -> dict:
     blk = max(128, (2_000_000_000 // pitch) // 128 * 128)
     stream = torch.cuda.Stream()
     prec = D.PREC_MIXED if a.precision == "mixed" else D.PREC_FP64
+    link0 = host_link_gbs(hv)
     with D.Handle(a.n_ind, a.n_snp, a.nrhs, precision=prec, stream=stream.cuda_stream, block_snps=blk) as h:
         h.upload(hv)
         h.set_omega(D.start_block(a.n_ind, a.nrhs))
@@ -454,9 +474,144 @@ def streamed_run(a, hv) -> dict:
         torch.cuda.synchronize()
         h.synchronize()
         t = e0.elapsed_time(e1) / 1e3 / steps
+    link1 = host_link_gbs(hv)
+    gbs = hv.nbytes / t / 1e9
     return {"value": a.n_ind * a.n_snp / t, "unit": UNIT, "ms_per_pass": t * 1e3,
-            "h2d_gbs": hv.nbytes / t / 1e9, "block_snps": blk, "blocks": (a.n_snp + blk - 1) // blk,
-            "note": "rows in pinned host memory, two device blocks double-buffered on a copy stream"}
+            "h2d_gbs": gbs, "link_gbs_before_after": [link0, link1], "frac_of_link": gbs / max(link0, link1),
+            "block_snps": blk, "blocks": (a.n_snp + blk - 1) // blk,
+            "note": "the in-core matrix's rows in pinned host memory, streamed in ~2 GB blocks every pass; the "
+                    "link is measured with cudaMemcpyAsync from the same pinned buffer just before and after"}
+
+
+def converged_run(a, hv) -> dict:
+    """Wall time of whole PCAs of the in-core matrix through dpca_run_packed (pinned host rows,
+    the host-to-device copy inside), run to convergence: with the published runs' flags (crit 2,
+    tol 1e-3) and with the reference's code defaults (crit 1, tol 1e-3); nsv 20, nrhs 40, power 6,
+    bsize 10,000 (the out-of-core variant of the solver)."""
+    import distpca_gb300 as D
+
+    om0 = D.start_block(a.n_ind, a.nrhs)
+    out = {}
+    for name, crit in (("crit2_tol1e-3", 2), ("crit1_tol1e-3", 1)):
+        kw = dict(nsv=a.nrhs // 2, nrhs=a.nrhs, power=a.power, crit=crit, tol=1e-3, miter=100, bsize=10_000,
+                  verbose=0, precision="mixed")
+        t0 = time.perf_counter()
+        r = D.run_packed(hv, a.n_ind, omega0=om0, **kw)
+        t = time.perf_counter() - t0
+        out[name] = {"seconds": t, "its": r["its"], "passes": r["passes"],
+                     "genotype_passes_per_s": a.n_ind * a.n_snp * r["passes"] / t,
+                     "load_s": r["time_load_matrix"], "sigma_1": float(r["sigma"][0])}
+    return out
+
+
+def config1_run(a) -> dict:
+    """The 1,000 x 100,000 workload the reference runs on a CPU (Balding-Nichols K = 5 x 200,
+    Fst 0.05, p ~ U(0.05, 0.5), 1% missing, seed 0; nsv 10, nrhs 20, power 4, tol 1e-6, bsize
+    10,000): the whole PCA through dpca_run_packed from pinned host rows, in both precisions, and
+    the CPU restatement of the reference on all host cores for three outer iterations, scaled to
+    the iterations the FP64 run took (the full CPU run takes minutes)."""
+    import torch
+
+    import distpca_gb300 as D
+    from distpca_gb300 import synth
+
+    n_ind, n_snp = 1000, 100_000
+    c = synth.make_cohort(n_ind, n_snp, n_pop=5, pop_sizes=[200] * 5, fst=0.05, p_range=(0.05, 0.5), missing=0.01,
+                          seed=0)
+    host = torch.empty((n_snp, (n_ind + 3) // 4), dtype=torch.uint8, pin_memory=True)
+    hv = host.numpy()
+    with D.Handle(n_ind, n_snp, 1, precision="fp64") as h:
+        h.synth_fill(c)
+        D.lib().dpca_download_packed(h._h, 0, n_snp, hv.ctypes.data)
+    kw = dict(nsv=10, nrhs=20, power=4, crit=1, tol=1e-6, miter=100, bsize=10_000, verbose=0)
+    om0 = D.start_block(n_ind, 20)
+    out = {"workload": "1000 x 100000, nsv 10, nrhs 20, power 4, crit 1, tol 1e-6, bsize 10000"}
+    for prec in ("mixed", "fp64"):
+        D.run_packed(hv, n_ind, omega0=om0, miter=1, **{k: v for k, v in kw.items() if k != "miter"},
+                     precision=prec)  # warm-up
+        t0 = time.perf_counter()
+        r = D.run_packed(hv, n_ind, omega0=om0, precision=prec, **kw)
+        t = time.perf_counter() - t0
+        out[prec] = {"seconds_per_pca": t, "its": r["its"], "passes": r["passes"],
+                     "genotype_passes_per_s": n_ind * n_snp * r["passes"] / t}
+    if not a.no_cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        t0 = time.perf_counter()
+        O.solve(hv, n_ind, nsv=10, nrhs=20, power=4, crit=1, tol=-1.0, miter=3, bsize=10_000, omega0=om0)
+        t3 = time.perf_counter() - t0
+        its = out["fp64"]["its"]
+        out["cpu_reference_port"] = {"seconds_3_iterations": t3, "seconds_per_pca_estimate": t3 / 3 * its,
+                                     "cores": threads, "kind": "port",
+                                     "note": f"3 outer iterations timed, scaled to the {its} iterations of the run"}
+        out["fp64_speedup_vs_cpu"] = out["cpu_reference_port"]["seconds_per_pca_estimate"] / out["fp64"]["seconds_per_pca"]
+        out["mixed_speedup_vs_cpu"] = out["cpu_reference_port"]["seconds_per_pca_estimate"] / out["mixed"]["seconds_per_pca"]
+    return out
+
+
+def out_of_core_run(a) -> dict:
+    """The out-of-core shape: 500,000 individuals x `ooc_snps` SNPs (250 GB packed at 2,000,000,
+    more than this machine's host memory), nrhs 20, mixed precision, streamed from pinned host memory
+    in ~2 GB SNP blocks every pass.  The rows come from a block source (dpca_upload_blocks) that
+    cycles over `ooc_distinct` distinct ~2 GB blocks of a seeded Balding-Nichols cohort (K = 10,
+    Fst 0.01, p ~ Beta(0.5, 2) clipped to [0.005, 0.5], 5% missing in 10% of the samples): a
+    matrix whose SNP blocks repeat, which costs the stream and the products exactly what distinct
+    blocks would.  The host link is measured with cudaMemcpyAsync from the same pinned blocks
+    just before and after the timed passes."""
+    import torch
+
+    import distpca_gb300 as D
+    from distpca_gb300 import synth
+
+    n_ind, n_snp, k = 500_000, a.ooc_snps, 20
+    npb = (n_ind + 3) // 4
+    pitch = (npb + 127) // 128 * 128
+    blk = max(128, (2_000_000_000 // pitch) // 128 * 128)
+    dist = max(1, min(a.ooc_distinct, (n_snp + blk - 1) // blk))
+    c = synth.make_cohort(n_ind, dist * blk, n_pop=10, fst=0.01, p_beta=(0.5, 2.0), p_clip=(0.005, 0.5),
+                          missing=0.05, heavy_frac=0.1, heavy_rate=0.05, seed=3)
+    host = torch.empty((dist * blk, npb), dtype=torch.uint8, pin_memory=True)
+    hv = host.numpy()
+    with D.Handle(n_ind, dist * blk, 1, precision="fp64") as h:
+        h.synth_fill(c)
+        D.lib().dpca_download_packed(h._h, 0, dist * blk, hv.ctypes.data)
+    torch.cuda.empty_cache()
+    base = hv.ctypes.data
+
+    def rows(s0, n):
+        j = (s0 // blk) % dist
+        return base + j * blk * npb, npb
+
+    link0 = host_link_gbs(hv)
+    stream = torch.cuda.Stream()
+    with D.Handle(n_ind, n_snp, k, precision="mixed", stream=stream.cuda_stream, block_snps=blk) as h:
+        h.upload_blocks(rows, max_row_stride=npb)  # the statistics sweep reads every block once
+        h.set_omega(D.start_block(n_ind, k))
+        h.pass_()
+        h.synchronize()
+        h.reset_kernel_times(True)
+        steps = 2
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            h.pass_()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        h.synchronize()
+        kt = h.kernel_times()
+        t = e0.elapsed_time(e1) / 1e3 / steps
+    link1 = host_link_gbs(hv)
+    packed_bytes = n_snp * npb
+    gbs = packed_bytes / t / 1e9
+    return {"n_ind": n_ind, "n_snp": n_snp, "nrhs": k, "packed_gb": packed_bytes / 1e9, "value": n_ind * n_snp / t,
+            "unit": UNIT, "seconds_per_pass": t, "h2d_gbs": gbs, "link_gbs_before_after": [link0, link1],
+            "frac_of_link": gbs / max(link0, link1), "block_snps": blk, "blocks": (n_snp + blk - 1) // blk,
+            "distinct_blocks": dist,
+            "kernel_ms_per_pass": {kk: round(v["ms"] / steps, 2) for kk, v in kt.items()},
+            "note": "every pass copies all packed rows host-to-device (two device blocks, copy stream beside the "
+                    "compute stream); the kernel times overlap the copies"}
 
 
 def windows_run(a) -> dict:
@@ -501,7 +656,7 @@ def windows_run(a) -> dict:
             "data": "seeded Balding-Nichols cohort filled on the device"}
 
 
-def serve_run(a) -> dict:
+def serve_run(a, rate: float, n_jobs: int, compare: bool) -> dict:
     """The mixed-size job stream through the serving loop (dpca_serve_*): Poisson arrivals of
     seeded Balding-Nichols jobs (n_ind log-U[500, 20k], n_snp log-U[10k, 500k], nsv in {5, 10, 20},
     nrhs 2 nsv, power 4; the reference's defaults crit 1, tol 1e-3), each job's genotypes filled
@@ -511,7 +666,7 @@ def serve_run(a) -> dict:
     import distpca_gb300 as D
     from distpca_gb300 import synth
 
-    jobs = synth.serve_stream(a.serve_jobs, a.serve_rate, seed=0)
+    jobs = synth.serve_stream(n_jobs, rate, seed=0)
     cohorts = [synth.serve_cohort(j) for j in jobs]
 
     def flags(j, prec):
@@ -542,27 +697,33 @@ def serve_run(a) -> dict:
                 out.append(r["info"].t_done - r["info"].t_start)
         return float(sum(out))
 
-    t64, tmx = one_at_a_time("fp64"), one_at_a_time("mixed")
-    return {"jobs": len(jobs), "arrival_rate_per_s": a.serve_rate, "slots": a.serve_slots,
-            "wall_s": wall, "jobs_per_s": len(jobs) / wall, "latency_p50_s": float(np.median(lat)),
-            "latency_p99_s": float(np.quantile(lat, 0.99)), "service_p50_s": float(np.median(svc)),
-            "genotype_passes_per_s": gpass / wall, "max_in_flight": st["max_in_flight"],
-            "peak_device_gb": st["peak_gb"], "budget_gb": st["budget_gb"],
-            "one_at_a_time": {"sample": f"jobs {picked} of the stream (the first {len(picked)} of <= 2e8 genotypes)",
-                              "fp64_gpu_s": t64, "mixed_s": tmx, "fp64_jobs_per_s": len(picked) / t64,
-                              "mixed_jobs_per_s": len(picked) / tmx},
-            "data": "seeded Balding-Nichols cohorts filled on the device per job"}
+    out = {"jobs": len(jobs), "arrival_rate_per_s": rate, "slots": a.serve_slots,
+           "wall_s": wall, "jobs_per_s": len(jobs) / wall, "latency_p50_s": float(np.median(lat)),
+           "latency_p99_s": float(np.quantile(lat, 0.99)), "service_p50_s": float(np.median(svc)),
+           "service_p99_s": float(np.quantile(svc, 0.99)),
+           "genotype_passes_per_s": gpass / wall, "max_in_flight": st["max_in_flight"],
+           "peak_device_gb": st["peak_gb"], "budget_gb": st["budget_gb"],
+           "data": "seeded Balding-Nichols cohorts filled on the device per job"}
+    if compare:
+        t64, tmx = one_at_a_time("fp64"), one_at_a_time("mixed")
+        out["one_at_a_time"] = {"sample": f"jobs {picked} of the stream (the first {len(picked)} of <= 2e8 genotypes)",
+                                "fp64_gpu_s": t64, "mixed_s": tmx, "fp64_jobs_per_s": len(picked) / t64,
+                                "mixed_jobs_per_s": len(picked) / tmx}
+    return out
 
 
-def cpu_baseline(a, hv) -> dict:
+def cpu_baseline_rows(a) -> dict:
+    from distpca_gb300 import synth
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
     O.set_threads(threads)
     S = min(a.cpu_snps, a.n_snp)
+    c = synth.config_cohort("incore50k", n_snp=a.n_snp, n_ind=a.n_ind)
+    sample = O.synth_rows(c, 0, S)  # the first S rows of the same matrix
     om = O.omega(a.n_ind, a.nrhs)
     walls = []
-    O.one_pass(np.ascontiguousarray(hv[:S]), a.n_ind, om, bsize=min(10_000, S), npasses=2, walls=walls)
+    O.one_pass(sample, a.n_ind, om, bsize=min(10_000, S), npasses=2, walls=walls)
     return {"value": a.n_ind * S / walls[-1], "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{S} SNPs x {a.n_ind} individuals, one steady-state pass (bsize 10000), OpenBLAS "
                       f"{threads} threads"}
