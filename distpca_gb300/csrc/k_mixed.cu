@@ -120,6 +120,9 @@ struct GemmArgs {
 // copies, MMAs) to finish: far longer than either takes.
 constexpr long long kExitCycles = 4000000;
 
+struct Handle;
+static int default_xty_cluster(const Handle *h);
+
 struct MixedState {
     int kp = 0, N = 0;
     __half *omega_s = nullptr;  // [N][n_ind_pad]
@@ -134,7 +137,10 @@ struct MixedState {
     int ring1 = 2, ring2 = 2;
     size_t smem1 = 0, smem2 = 0;
     int splits_cap = 1;          // partial buffer capacity (splits)
+    int xty_cl = 0;              // X^T Y cluster width (1, 2 or 4: the dense operand is multicast; 0: by item length)
+    int max_clusters[3] = {0, 0, 0};  // co-resident X^T Y clusters of width 1, 2, 4 (0: not queried)
     CUtensorMap map_p[2], map_pt[2], map_om, map_bop;  // [1]: second block buffer when streaming
+    CUtensorMap map_bop_band[2];  // map_bop with one K-block, 2N/2 and 2N/4 rows per box (clusters of 2 and 4)
 };
 
 // ------------------------------------------------------------------ decode
@@ -286,10 +292,20 @@ __device__ __forceinline__ WorkItem work_item(const GemmArgs &a, int it) {
     return x;
 }
 
-template <int MODE>
+// CL > 1 (X^T Y only): the kernel runs in clusters of CL CTAs that walk consecutive row tiles of
+// the same K range in lockstep, and the dense operand (the same for all of them) is loaded once
+// per cluster: each CTA loads 1/CL of every B stage (a band of its rows, both K-blocks) and
+// multicasts it to the whole cluster, so the operand is read from L2 once per cluster instead
+// of once per CTA -- the L2-to-SM traffic of this operand, which bounds X^T Y, drops CL-fold.
+// A stage may be refilled only when every CTA of the cluster has consumed it, so the MMA
+// issuers' "stage free" commits are multicast to every CTA (free_ counts 2 CL commits).  The
+// CTAs meet at a cluster barrier after barrier initialisation (no remote arrival may reach an
+// uninitialised barrier) and before exit (no multicast may land in an exited CTA's memory).
+template <int MODE, int CL>
 __global__ void __launch_bounds__(kThreads, 1)
     mixed_gemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                       const GemmArgs args) {
+    static_assert(CL == 1 || (MODE == kXTY && (CL == 2 || CL == 4)), "multicast clusters: X^T Y, 2 or 4 CTAs");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int N = args.N, kp = args.kp, R = args.ring;
@@ -322,7 +338,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int s = 0; s < R; ++s) {
             tc::mbar_init(&full[s], 1 + 4);  // producer (with the TMA bytes) + the group's 4 decode warps
-            tc::mbar_init(&free_[s], 2);     // one commit per MMA issuer
+            tc::mbar_init(&free_[s], 2 * CL);  // one commit per MMA issuer of every CTA of the cluster
         }
         for (int v = 0; v < 2; ++v) {
             tc::mbar_init(&acc_full[v], 1);
@@ -340,8 +356,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     tc::fence_before_sync();
     __syncthreads();
+    if (CL > 1) tc::cluster_sync();
     tc::fence_after_sync();
     const uint32_t tbase = *tmem_slot;
+    // multicast band of this CTA: rows [rank * band, (rank + 1) * band) of each B tile
+    const int rank = CL > 1 ? (int)tc::cluster_ctarank() : 0;
+    const int band = rows_box / CL;
+    constexpr uint16_t kMask = (uint16_t)((1u << CL) - 1u);
     // TMEM columns: G' accumulator [0, N), M accumulator [N, 2N) (each [h | l] slices), then
     // the two A stages (decode group g owns [a_base + 128 g, +128): G' K-blocks 0-1, then M).
     const int a_base = (2 * N + 31) & ~31;
@@ -356,6 +377,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             uint32_t pph = 0, bph = 0;
             bool ok = true;
             bool withhold = args.inject == 1 && blockIdx.x == 0;
+            int withheld = 0;
             const long long lim = args.wait_cycles;
             for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
                 const WorkItem x = work_item(args, it);
@@ -364,9 +386,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if ((t & 3) == 0) {
                         if (!(ok = tc::mbar_wait(&pk_empty[sp], pph ^ 1, err, 11, true, lim))) break;
                         tc::mbar_arrive_expect_tx(&pk_full[sp], kPStageBytes);
-                        if (MODE == kXTY)  // tile-blocked: (row block, K tile) at row ((rb * nkt) + kt) * 128
+                        if (MODE == kXTY)  // tile-blocked: (row block, K tile) at row ((rb * nkt) + kt) * 128;
+                                           // a cluster's padding tile (no rows) reads the last real tile
                             tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], 0,
-                                            (x.tile * args.a_ktiles + ((x.kb0 + 2 * t) >> 3)) * 128);
+                                            (min(x.tile, (args.rows + 127) / 128 - 1) * args.a_ktiles +
+                                             ((x.kb0 + 2 * t) >> 3)) * 128);
                         else
                             tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (x.kb0 + 2 * t) * 16,
                                             x.tile * 128);
@@ -376,9 +400,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (!(ok = tc::mbar_wait(&free_[r], bph ^ 1, err, 12, true, lim))) break;
                     if (withhold) {
                         withhold = false;  // injected fault: this batch never arrives
+                        ++withheld;
                     } else {
-                        tc::mbar_arrive_expect_tx(&full[r], bstage);
-                        tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, b_row0, x.kb0 + 2 * t);
+                        tc::mbar_arrive_expect_tx(&full[r], bstage);  // all CL bands land here
+                        if (CL == 1) {
+                            tc::tma_load_3d(sB + (size_t)r * bstage, &map_b, &full[r], 0, b_row0, x.kb0 + 2 * t);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 2; ++j)
+                                tc::tma_load_3d_mc(sB + (size_t)r * bstage + j * tile_bytes + rank * band * 128, &map_b,
+                                                   &full[r], 0, rank * band, x.kb0 + 2 * t + j, kMask);
+                        }
                         ++issued_b;
                     }
                     if (++r == R) r = 0, bph ^= 1;
@@ -390,13 +422,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int g = max(0, issued_p - kPStages); g < issued_p; ++g)
                 if (!tc::mbar_wait(&pk_full[g % kPStages], (g / kPStages) & 1, err, 13, true, lim))
                     tc::mbar_wait_exit(&pk_full[g % kPStages], (g / kPStages) & 1, kExitCycles);
-            if (issued_b > 0) {
+            {
                 // batches are numbered by ring position; a withheld batch leaves a gap, so wait on
-                // the phases of the last min(R, issued) ring positions the producer reached
-                const int reached = issued_b + (args.inject == 1 && blockIdx.x == 0 ? 1 : 0);
+                // the phases of the last min(R, reached) ring positions the producer reached
+                const int reached = issued_b + withheld;
                 for (int t = max(0, reached - R); t < reached; ++t)
                     if (!tc::mbar_wait(&full[t % R], (t / R) & 1, err, 14, true, lim))
                         tc::mbar_wait_exit(&full[t % R], (t / R) & 1, kExitCycles);
+                // the cluster's stage-free commits for the last stages land on this CTA's barriers:
+                // wait for them too, so that no remote arrival is in flight when the CTA exits
+                if (CL > 1)
+                    for (int t = max(0, reached - R); t < reached; ++t)
+                        if (!tc::mbar_wait(&free_[t % R], (t / R) & 1, err, 15, true, lim))
+                            tc::mbar_wait_exit(&free_[t % R], (t / R) & 1, kExitCycles);
             }
         }
     } else if (warp == 1 || warp == kIssuerWarpM) {
@@ -440,7 +478,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     tc::mma_ts_f16(d, a + 40, b2 + 2, idesc, 1u);
                     tc::mma_ts_f16(d, a + 48, b2 + 4, idesc, 1u);
                     tc::mma_ts_f16(d, a + 56, b2 + 6, idesc, 1u);
-                    tc::mma_commit(&free_[r]);
+                    if (CL == 1) tc::mma_commit(&free_[r]);
+                    else tc::mma_commit_mc(&free_[r], kMask);
                     if (chunk_done) tc::mma_commit(&acc_full[v]);
                 }
                 __syncwarp();
@@ -636,6 +675,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     tc::fence_before_sync();
     __syncthreads();
+    if (CL > 1) tc::cluster_sync();
     tc::fence_after_sync();
     if (MODE == kXW && !args.tile_win && threadIdx.x < args.k && cmax_s[threadIdx.x] != 0u)
         atomicMax(args.colmax + threadIdx.x, cmax_s[threadIdx.x]);
@@ -910,7 +950,8 @@ static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base
 // K-blocks, each a rows x 128 B tile (n_pad is a multiple of 128, so whole batches exist).
 // FP16 operand [rows][n_pad] as 3-D boxes of box_rows rows x 2 K-blocks of 64 (box_rows = rows,
 // or the N rows of one window when the rows stack several windows' slices).
-static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, uint64_t rows, uint32_t box_rows = 0) {
+static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, uint64_t rows, uint32_t box_rows = 0,
+                                  uint32_t box_kblocks = 2) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) {
         set_error("cuTensorMapEncodeTiled unavailable");
@@ -918,7 +959,7 @@ static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, 
     }
     cuuint64_t dims[3] = {64, rows, n_pad / 64};
     cuuint64_t strides[2] = {n_pad * 2, 128};
-    cuuint32_t box[3] = {64, box_rows ? box_rows : (cuuint32_t)rows, 2};
+    cuuint32_t box[3] = {64, box_rows ? box_rows : (cuuint32_t)rows, box_kblocks};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -1029,8 +1070,13 @@ dpca_status mixed_prepare(Handle *h) {
     }
     DPCA_TRY(make_batch_map(&m->map_om, m->omega_s, h->n_ind_pad, N));
     DPCA_TRY(make_batch_map(&m->map_bop, m->bop, rows_pad, 2 * N));
-    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW>));
-    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY>));
+    DPCA_TRY(make_batch_map(&m->map_bop_band[0], m->bop, rows_pad, 2 * N, (uint32_t)N, 1));
+    DPCA_TRY(make_batch_map(&m->map_bop_band[1], m->bop, rows_pad, 2 * N, (uint32_t)(N / 2), 1));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW, 1>));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 1>));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 2>));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 4>));
+    m->xty_cl = default_xty_cluster(h);
     return DPCA_OK;
 }
 
@@ -1103,7 +1149,7 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
         a.tiles = a.items = ceil_div(rows, 128);
-        mixed_gemm_kernel<kXW><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(map_a, m->map_om, a);
+        mixed_gemm_kernel<kXW, 1><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(map_a, m->map_om, a);
         DPCA_CUDA(cudaGetLastError());
     }
     ScopedLaunch t(&h->clock, h->stream, "split_bop");
@@ -1113,6 +1159,70 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
                                                    m->bop, m->rq);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
+}
+
+// Cluster width of X^T Y when nothing chose one (0): pairs of CTAs sharing each dense-operand
+// stage for long work items, where that operand's L2-to-SM traffic bounds the kernel (measured at
+// 50,000 x 1,000,000, k = 40: 15.9 ms alone, 11.2 ms in pairs, 12.3 ms in fours); single CTAs for
+// short items, whose persistent grid loses more to cluster scheduling than it saves (5,000 x
+// 300,000: 0.30 ms alone, 0.31 in pairs, 0.37 in fours).  DPCA_XTY_CLUSTER = 1, 2 or 4 overrides.
+static int default_xty_cluster(const Handle *h) {
+    (void)h;
+    if (const char *e = getenv("DPCA_XTY_CLUSTER")) {
+        const int v = atoi(e);
+        if (v == 1 || v == 2 || v == 4) return v;
+    }
+    return 0;
+}
+
+template <int CL>
+static dpca_status launch_xty_cl(Handle *h, const CUtensorMap &map_a, GemmArgs a, int splits, int batches_per_item) {
+    MixedState *m = mstate(h);
+    a.tiles = (ceil_div(h->n_ind, 128) + CL - 1) / CL * CL;  // whole clusters: padding tiles have no rows
+    a.items = a.tiles * splits;
+    int grid = xty_grid(h, a.items, batches_per_item);
+    if (CL == 1) {
+        mixed_gemm_kernel<kXTY, 1><<<grid, kThreads, m->smem2, h->stream>>>(map_a, m->map_bop, a);
+        DPCA_CUDA(cudaGetLastError());
+        return DPCA_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = m->smem2;
+    cfg.stream = h->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int &maxc = m->max_clusters[CL == 2 ? 1 : 2];
+    if (maxc == 0) {
+        cfg.gridDim = dim3(CL * h->sm_count);
+        DPCA_CUDA(cudaOccupancyMaxActiveClusters(&maxc, mixed_gemm_kernel<kXTY, CL>, &cfg));
+        if (maxc < 1) {
+            set_error("X^T Y: no cluster of %d CTAs fits on this device", CL);
+            return DPCA_ERR_UNSUPPORTED;
+        }
+    }
+    // a persistent grid (short items) holds as many clusters as can run at once
+    if (grid < a.items) grid = std::min(a.items, maxc * CL);
+    grid = (grid + CL - 1) / CL * CL;
+    cfg.gridDim = dim3(grid);
+    DPCA_CUDA(cudaLaunchKernelEx(&cfg, mixed_gemm_kernel<kXTY, CL>, map_a, m->map_bop_band[CL == 2 ? 0 : 1], a));
+    return DPCA_OK;
+}
+
+static dpca_status launch_xty(Handle *h, const CUtensorMap &map_a, const GemmArgs &a, int splits,
+                              int batches_per_item) {
+    int cl = mstate(h)->xty_cl;
+    if (cl == 0) cl = batches_per_item > 128 && ceil_div(h->n_ind, 128) >= 2 ? 2 : 1;
+    switch (cl) {
+        case 2: return launch_xty_cl<2>(h, map_a, a, splits, batches_per_item);
+        case 4: return launch_xty_cl<4>(h, map_a, a, splits, batches_per_item);
+        default: return launch_xty_cl<1>(h, map_a, a, splits, batches_per_item);
+    }
 }
 
 // Z (+)= X^T Y over `nsnp` SNPs (individual-major operand behind map_a, Y operand in m->bop).
@@ -1139,11 +1249,7 @@ static dpca_status xty_rows(Handle *h, const CUtensorMap &map_a, int nsnp, doubl
     a.err = h->dflag;
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xty");
-        a.tiles = ceil_div(h->n_ind, 128);
-        a.items = a.tiles * splits;
-        mixed_gemm_kernel<kXTY><<<xty_grid(h, a.items, kb_per_split / 2), kThreads, m->smem2, h->stream>>>(
-            map_a, m->map_bop, a);
-        DPCA_CUDA(cudaGetLastError());
+        DPCA_TRY(launch_xty(h, map_a, a, splits, kb_per_split / 2));
     }
     ScopedLaunch t(&h->clock, h->stream, "mixed_reduce");
     int64_t elems = (int64_t)h->n_ind * k;
@@ -1191,7 +1297,7 @@ dpca_status mixed_win_pass(Handle *h, const WinPass &p) {
     {
         ScopedLaunch t(&h->clock, h->stream, "win_mixed_xw");
         a.tiles = a.items = ceil_div(rows, 128);
-        mixed_gemm_kernel<kXW><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(m->map_p[0], *p.map_om,
+        mixed_gemm_kernel<kXW, 1><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(m->map_p[0], *p.map_om,
                                                                                                  a);
         DPCA_CUDA(cudaGetLastError());
     }
@@ -1223,7 +1329,7 @@ dpca_status mixed_win_pass(Handle *h, const WinPass &p) {
         ScopedLaunch t(&h->clock, h->stream, "win_mixed_xty");
         b.tiles = ceil_div(n, 128);
         b.items = b.tiles * p.W;
-        mixed_gemm_kernel<kXTY><<<xty_grid(h, b.items, ceil_div(rows, 128 * p.W)), kThreads, m->smem2, h->stream>>>(
+        mixed_gemm_kernel<kXTY, 1><<<xty_grid(h, b.items, ceil_div(rows, 128 * p.W)), kThreads, m->smem2, h->stream>>>(
             m->map_pt[0],
                                                                                                  m->map_bop, b);
         DPCA_CUDA(cudaGetLastError());
