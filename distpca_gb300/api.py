@@ -110,6 +110,7 @@ _SIGS = {
     "dpca_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
     "dpca_upload_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "dpca_inject_fault": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]),
+    "dpca_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "dpca_upload_blocks": (ctypes.c_int, [ctypes.c_void_p, BLOCK_FN, ctypes.c_void_p, ctypes.c_int64]),
     "dpca_synth_fill": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_int]),
@@ -344,6 +345,14 @@ class Handle:
 
     def upload_ptr(self, ptr: int, row_stride: int) -> None:
         _check(lib().dpca_upload(self._h, ctypes.c_void_p(ptr), row_stride))
+
+    def autotune(self) -> Dict:
+        """Tune the product kernels' launch parameters on this handle (see dpca_autotune)."""
+        import json
+
+        buf = ctypes.create_string_buffer(1024)
+        _check(lib().dpca_autotune(self._h, buf, 1024))
+        return json.loads(buf.value.decode())
 
     def inject_fault(self, fault: int = 1, wait_limit_ms: float = 1.0) -> None:
         """Test hook: the next mixed X Omega launch withholds one load; its bounded wait runs out."""

@@ -56,6 +56,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
 
 #include "common.cuh"
 #include "dpca_internal.h"
@@ -121,7 +127,11 @@ struct GemmArgs {
 constexpr long long kExitCycles = 4000000;
 
 struct Handle;
+struct GemmArgs;
 static int default_xty_cluster(const Handle *h);
+static void apply_tuned(Handle *h);
+static dpca_status launch_xw(Handle *h, const CUtensorMap &map_a, const CUtensorMap &map_b,
+                             const CUtensorMap &map_b_band, GemmArgs a);
 
 struct MixedState {
     int kp = 0, N = 0;
@@ -138,9 +148,13 @@ struct MixedState {
     size_t smem1 = 0, smem2 = 0;
     int splits_cap = 1;          // partial buffer capacity (splits)
     int xty_cl = 0;              // X^T Y cluster width (1, 2 or 4: the dense operand is multicast; 0: by item length)
+    int xty_persistent = -1;     // X^T Y grid: 1 persistent, 0 one CTA per item, -1 by item length
     int max_clusters[3] = {0, 0, 0};  // co-resident X^T Y clusters of width 1, 2, 4 (0: not queried)
     CUtensorMap map_p[2], map_pt[2], map_om, map_bop;  // [1]: second block buffer when streaming
     CUtensorMap map_bop_band[2];  // map_bop with one K-block, 2N/2 and 2N/4 rows per box (clusters of 2 and 4)
+    CUtensorMap map_om_band;      // map_om with one K-block and N/2 rows per box (X Omega in pairs)
+    int xw_cl = 0;                // X Omega cluster width (1 or 2; 0: by tile count)
+    int xw_max_clusters = 0;      // co-resident X Omega pairs (0: not queried)
 };
 
 // ------------------------------------------------------------------ decode
@@ -284,7 +298,7 @@ __device__ __forceinline__ WorkItem work_item(const GemmArgs &a, int it) {
     WorkItem x;
     x.tile = it % a.tiles;
     x.split = it / a.tiles;
-    x.win = a.tile_win ? a.tile_win[x.tile] : (a.win_kb0 ? x.split : 0);
+    x.win = a.tile_win ? a.tile_win[min(x.tile, (a.rows + 127) / 128 - 1)] : (a.win_kb0 ? x.split : 0);
     const bool skip = (a.tile_win || a.win_kb0) && a.win_active && !a.win_active[x.win];
     x.kb0 = a.win_kb0 ? a.win_kb0[x.split] : x.split * a.kb_per_split;
     const int nkb = a.win_kb0 ? a.win_nkb[x.split] : min(a.nkb_total, x.kb0 + a.kb_per_split) - x.kb0;
@@ -292,9 +306,9 @@ __device__ __forceinline__ WorkItem work_item(const GemmArgs &a, int it) {
     return x;
 }
 
-// CL > 1 (X^T Y only): the kernel runs in clusters of CL CTAs that walk consecutive row tiles of
-// the same K range in lockstep, and the dense operand (the same for all of them) is loaded once
-// per cluster: each CTA loads 1/CL of every B stage (a band of its rows, both K-blocks) and
+// CL > 1: the kernel runs in clusters of CL CTAs that walk consecutive row tiles of the same K
+// range in lockstep (X Omega: consecutive SNP tiles, which all read the same Omega slices), and
+// the dense operand (the same for all of them) is loaded once per cluster: each CTA loads 1/CL of every B stage (a band of its rows, both K-blocks) and
 // multicasts it to the whole cluster, so the operand is read from L2 once per cluster instead
 // of once per CTA -- the L2-to-SM traffic of this operand, which bounds X^T Y, drops CL-fold.
 // A stage may be refilled only when every CTA of the cluster has consumed it, so the MMA
@@ -305,7 +319,7 @@ template <int MODE, int CL>
 __global__ void __launch_bounds__(kThreads, 1)
     mixed_gemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                       const GemmArgs args) {
-    static_assert(CL == 1 || (MODE == kXTY && (CL == 2 || CL == 4)), "multicast clusters: X^T Y, 2 or 4 CTAs");
+    static_assert(CL == 1 || CL == 2 || (MODE == kXTY && CL == 4), "multicast clusters: 2 CTAs, or 4 for X^T Y");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int N = args.N, kp = args.kp, R = args.ring;
@@ -393,7 +407,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                              ((x.kb0 + 2 * t) >> 3)) * 128);
                         else
                             tc::tma_load_2d(sP + sp * kPStageBytes, &map_a, &pk_full[sp], (x.kb0 + 2 * t) * 16,
-                                            x.tile * 128);
+                                            min(x.tile, (args.rows + 127) / 128 - 1) * 128);
                         ++issued_p;
                         if (++sp == kPStages) sp = 0, pph ^= 1;
                     }
@@ -409,7 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                             for (int j = 0; j < 2; ++j)
                                 tc::tma_load_3d_mc(sB + (size_t)r * bstage + j * tile_bytes + rank * band * 128, &map_b,
-                                                   &full[r], 0, rank * band, x.kb0 + 2 * t + j, kMask);
+                                                   &full[r], 0, b_row0 + rank * band, x.kb0 + 2 * t + j, kMask);
                         }
                         ++issued_b;
                     }
@@ -986,8 +1000,10 @@ static size_t fixed_bytes(int mode, int kp) {
 // (tens of MB each) then no longer share L2, while the hardware scheduler keeps concurrently
 // running CTAs on neighbouring items (measured at 50,000 x 1,000,000: 19.5 ms persistent vs
 // 15.9 ms one CTA per item).  X Omega shares one L2-resident operand and is always persistent.
-static int xty_grid(const Handle *h, int items, int batches_per_item) {
-    return batches_per_item > 128 ? items : std::min(items, h->sm_count);
+static int xty_grid(Handle *h, int items, int batches_per_item) {
+    const int mode = h->mx ? mstate(h)->xty_persistent : -1;
+    const bool per_item = mode < 0 ? batches_per_item > 128 : mode == 0;
+    return per_item ? items : std::min(items, h->sm_count);
 }
 
 static int pick_ring(int mode, int N, int kp) {
@@ -1070,13 +1086,16 @@ dpca_status mixed_prepare(Handle *h) {
     }
     DPCA_TRY(make_batch_map(&m->map_om, m->omega_s, h->n_ind_pad, N));
     DPCA_TRY(make_batch_map(&m->map_bop, m->bop, rows_pad, 2 * N));
+    DPCA_TRY(make_batch_map(&m->map_om_band, m->omega_s, h->n_ind_pad, N, (uint32_t)(N / 2), 1));
     DPCA_TRY(make_batch_map(&m->map_bop_band[0], m->bop, rows_pad, 2 * N, (uint32_t)N, 1));
     DPCA_TRY(make_batch_map(&m->map_bop_band[1], m->bop, rows_pad, 2 * N, (uint32_t)(N / 2), 1));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW, 1>));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW, 2>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 1>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 2>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 4>));
     m->xty_cl = default_xty_cluster(h);
+    apply_tuned(h);
     return DPCA_OK;
 }
 
@@ -1148,9 +1167,7 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     DPCA_CUDA(cudaMemsetAsync(m->rq, 0, (size_t)k * 8, h->stream));
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
-        a.tiles = a.items = ceil_div(rows, 128);
-        mixed_gemm_kernel<kXW, 1><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(map_a, m->map_om, a);
-        DPCA_CUDA(cudaGetLastError());
+        DPCA_TRY(launch_xw(h, map_a, m->map_om, m->map_om_band, a));
     }
     ScopedLaunch t(&h->clock, h->stream, "split_bop");
     const int n128 = (rows + 127) & ~127;
@@ -1161,13 +1178,60 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     return DPCA_OK;
 }
 
+// X Omega launch: a persistent grid of single CTAs, or of pairs that share each Omega-slice stage
+// by multicast (the slices, re-read by every SNP tile, stream ~62 GB from L2 per pass at 50,000 x
+// 1,000,000, k = 40).  Pairs are the autotuner's to choose: at that shape a copy of the kernel
+// without the decode, the tensor-memory stores and the MMAs took 6.2 ms, bound by those slice
+// loads, but the whole kernel measured 10.84 ms single and 10.99 ms in pairs -- its limit is the
+// decode-to-MMA handoff, not the slices.  DPCA_XW_CLUSTER = 1 or 2 overrides the choice.
+static dpca_status launch_xw(Handle *h, const CUtensorMap &map_a, const CUtensorMap &map_b,
+                             const CUtensorMap &map_b_band, GemmArgs a) {
+    MixedState *m = mstate(h);
+    int cl = m->xw_cl;
+    if (const char *e = getenv("DPCA_XW_CLUSTER")) {
+        const int v = atoi(e);
+        if (v == 1 || v == 2) cl = v;
+    }
+    const int tiles = ceil_div(a.rows, 128);
+    if (cl == 0) cl = 1;
+    if (cl == 1 || tiles < 2) {
+        a.tiles = a.items = tiles;
+        mixed_gemm_kernel<kXW, 1><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(map_a, map_b, a);
+        DPCA_CUDA(cudaGetLastError());
+        return DPCA_OK;
+    }
+    a.tiles = a.items = (tiles + 1) / 2 * 2;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = m->smem1;
+    cfg.stream = h->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (m->xw_max_clusters == 0) {
+        cfg.gridDim = dim3(2 * h->sm_count);
+        DPCA_CUDA(cudaOccupancyMaxActiveClusters(&m->xw_max_clusters, mixed_gemm_kernel<kXW, 2>, &cfg));
+        if (m->xw_max_clusters < 1) {
+            set_error("X Omega: no pair of CTAs fits on this device");
+            return DPCA_ERR_UNSUPPORTED;
+        }
+    }
+    cfg.gridDim = dim3(std::min(a.items, 2 * m->xw_max_clusters));
+    DPCA_CUDA(cudaLaunchKernelEx(&cfg, mixed_gemm_kernel<kXW, 2>, map_a, map_b_band, a));
+    return DPCA_OK;
+}
+
 // Cluster width of X^T Y when nothing chose one (0): pairs of CTAs sharing each dense-operand
 // stage for long work items, where that operand's L2-to-SM traffic bounds the kernel (measured at
 // 50,000 x 1,000,000, k = 40: 15.9 ms alone, 11.2 ms in pairs, 12.3 ms in fours); single CTAs for
 // short items, whose persistent grid loses more to cluster scheduling than it saves (5,000 x
 // 300,000: 0.30 ms alone, 0.31 in pairs, 0.37 in fours).  DPCA_XTY_CLUSTER = 1, 2 or 4 overrides.
 static int default_xty_cluster(const Handle *h) {
-    (void)h;
+    (void)h;  // (a tuned choice for the handle's shape class is applied by mixed_prepare)
     if (const char *e = getenv("DPCA_XTY_CLUSTER")) {
         const int v = atoi(e);
         if (v == 1 || v == 2 || v == 4) return v;
@@ -1329,10 +1393,7 @@ dpca_status mixed_win_pass(Handle *h, const WinPass &p) {
         ScopedLaunch t(&h->clock, h->stream, "win_mixed_xty");
         b.tiles = ceil_div(n, 128);
         b.items = b.tiles * p.W;
-        mixed_gemm_kernel<kXTY, 1><<<xty_grid(h, b.items, ceil_div(rows, 128 * p.W)), kThreads, m->smem2, h->stream>>>(
-            m->map_pt[0],
-                                                                                                 m->map_bop, b);
-        DPCA_CUDA(cudaGetLastError());
+        DPCA_TRY(launch_xty(h, m->map_pt[0], b, p.W, ceil_div(rows, 128 * p.W)));
     }
     {
         ScopedLaunch t(&h->clock, h->stream, "win_reduce");
@@ -1364,4 +1425,189 @@ dpca_status mixed_block(Handle *h, int b, int s0, int ns, double *z, bool accumu
     return xty_rows(h, m->map_pt[b], ns, z, accumulate);
 }
 
+// ------------------------------------------------------------------ autotuner
+// The product kernels' launch parameters -- X^T Y's cluster width (1, 2, 4), grid mode
+// (persistent or one CTA per work item), K-split count and B-ring depth, and X Omega's cluster
+// width (1, 2) and B-ring depth -- measured on a handle's own matrix, choice by choice, with CUDA
+// events on its stream, and remembered for the handle's shape class (individual tiles, SNP
+// K-blocks, padded width k, each class one octave wide), so that later handles of the class
+// (serving jobs, repeated solves) start from the measured choice.  The heuristics (pick_splits,
+// pick_ring, the cluster and grid rules) are what a shape class without a measurement uses.
+struct TuneChoice {
+    int xty_cl = 0, xty_persistent = -1, kb_per_split = 0, ring1 = 0, ring2 = 0, xw_cl = 0;
+};
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int>, TuneChoice> g_tune;
+
+static std::tuple<int, int, int> tune_class(const Handle *h) {
+    auto oct = [](int v) { return v <= 1 ? 0 : (int)std::ceil(std::log2((double)v)); };
+    return std::make_tuple(oct(ceil_div(h->n_ind, 128)), oct(ceil_div(h->rows_dev, 64)), (h->k + 7) / 8 * 8);
+}
+
+static void set_rings(Handle *h, int ring1, int ring2) {
+    MixedState *m = mstate(h);
+    const int max1 = pick_ring(kXW, m->N, m->kp), max2 = pick_ring(kXTY, m->N, m->kp);
+    m->ring1 = std::max(2, std::min(ring1, max1));
+    m->ring2 = std::max(2, std::min(ring2, max2));
+    m->smem1 = smem_bytes(kXW, m->N, m->kp, m->ring1);
+    m->smem2 = smem_bytes(kXTY, m->N, m->kp, m->ring2);
+}
+
+static void apply_tuned(Handle *h) {
+    if (h->streamed) return;
+    TuneChoice c;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(tune_class(h));
+        if (it == g_tune.end()) return;
+        c = it->second;
+    }
+    MixedState *m = mstate(h);
+    if (getenv("DPCA_XTY_CLUSTER") == nullptr) m->xty_cl = c.xty_cl;
+    m->xw_cl = c.xw_cl;
+    m->xty_persistent = c.xty_persistent;
+    const int nkb = ceil_div(h->n_snp, 64);
+    if (c.kb_per_split > 0 && ceil_div(nkb, c.kb_per_split) <= m->splits_cap) {
+        m->kb_per_split = c.kb_per_split;
+        m->splits = ceil_div(nkb, c.kb_per_split);
+    }
+    set_rings(h, c.ring1, c.ring2);
+}
+
+// Mean device time of `reps` runs of f after one warm-up run, on the handle's stream.
+template <typename F>
+static dpca_status time_runs(Handle *h, int reps, F f, double *ms) {
+    DPCA_TRY(f());
+    cudaEvent_t a = nullptr, b = nullptr;
+    DPCA_CUDA(cudaEventCreate(&a));
+    DPCA_CUDA(cudaEventCreate(&b));
+    dpca_status st = DPCA_OK;
+    if (cudaEventRecord(a, h->stream) != cudaSuccess) st = DPCA_ERR_CUDA;
+    for (int i = 0; i < reps && st == DPCA_OK; ++i) st = f();
+    float t = 0.f;
+    if (st == DPCA_OK && (cudaEventRecord(b, h->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                          cudaEventElapsedTime(&t, a, b) != cudaSuccess)) {
+        set_error("autotune: event timing failed");
+        st = DPCA_ERR_CUDA;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = t / reps;
+    return st;
+}
+
+static dpca_status autotune_impl(Handle *h, std::string *report) {
+    if (h->precision != DPCA_PREC_MIXED || h->streamed || !h->stats_ready) {
+        set_error("dpca_autotune: needs a resident mixed-precision handle with its rows uploaded");
+        return DPCA_ERR_INVALID;
+    }
+    MixedState *m = mstate(h);
+    const int reps = 2;
+    auto run_xw = [&]() { return launch_mixed_xw(h, h->omega, nullptr); };
+    auto run_xty = [&]() { return launch_mixed_xty(h, h->z); };
+    const int max1 = pick_ring(kXW, m->N, m->kp), max2 = pick_ring(kXTY, m->N, m->kp);
+    const TuneChoice def{m->xty_cl, m->xty_persistent, m->kb_per_split, m->ring1, m->ring2, m->xw_cl};
+    TuneChoice b = def;
+    // X Omega: cluster width, then B-ring depth
+    double def_xw = 0, best_xw = 0;
+    DPCA_TRY(time_runs(h, reps, run_xw, &def_xw));
+    best_xw = def_xw;
+    const int tiles1 = ceil_div(h->n_snp, 128);
+    for (int cl : {1, 2}) {
+        if (cl == 2 && tiles1 < 2) continue;
+        m->xw_cl = cl;
+        double t = 0;
+        DPCA_TRY(time_runs(h, reps, run_xw, &t));
+        if (t < best_xw * 0.98) best_xw = t, b.xw_cl = cl;
+    }
+    m->xw_cl = b.xw_cl;
+    for (int r1 : {2, 3, max1}) {
+        if (r1 > max1 || r1 == b.ring1) continue;
+        set_rings(h, r1, m->ring2);
+        double t = 0;
+        DPCA_TRY(time_runs(h, reps, run_xw, &t));
+        if (t < best_xw * 0.98) best_xw = t, b.ring1 = r1;
+    }
+    set_rings(h, b.ring1, m->ring2);
+    DPCA_TRY(run_xw());  // the Y operand for the X^T Y trials
+    // X^T Y stage 1: cluster width x grid mode
+    double def_xty = 0, best = 0;
+    DPCA_TRY(time_runs(h, reps, run_xty, &def_xty));
+    best = def_xty;
+    const int tiles = ceil_div(h->n_ind, 128);
+    for (int cl : {1, 2, 4}) {
+        if (cl > 1 && tiles < cl) continue;
+        for (int pers : {0, 1}) {
+            m->xty_cl = cl;
+            m->xty_persistent = pers;
+            double t = 0;
+            DPCA_TRY(time_runs(h, reps, run_xty, &t));
+            if (t < best * 0.98) best = t, b.xty_cl = cl, b.xty_persistent = pers;
+        }
+    }
+    m->xty_cl = b.xty_cl;
+    m->xty_persistent = b.xty_persistent;
+    // stage 2: K-split counts with good wave efficiency (within the partial buffer)
+    const int nkb = ceil_div(h->n_snp, 64), ngroups = ceil_div(nkb, 8);
+    std::vector<std::pair<double, int>> cands;
+    for (int sp = 1; sp <= std::min(16, ngroups); ++sp) {
+        const int kbps = 8 * ceil_div(ngroups, sp), sreal = ceil_div(nkb, kbps);
+        if (sreal > m->splits_cap) continue;
+        const int64_t items = (int64_t)tiles * sreal;
+        const double eff = (double)items / (double)(h->sm_count * ((items + h->sm_count - 1) / h->sm_count));
+        bool dup = false;
+        for (auto &c : cands) dup = dup || c.second == kbps;
+        if (!dup) cands.push_back({-eff, kbps});
+    }
+    std::sort(cands.begin(), cands.end());
+    for (size_t i = 0; i < cands.size() && i < 4; ++i) {
+        const int kbps = cands[i].second;
+        if (kbps == b.kb_per_split) continue;
+        m->kb_per_split = kbps;
+        m->splits = ceil_div(nkb, kbps);
+        double t = 0;
+        DPCA_TRY(time_runs(h, reps, run_xty, &t));
+        if (t < best * 0.98) best = t, b.kb_per_split = kbps;
+    }
+    m->kb_per_split = b.kb_per_split;
+    m->splits = ceil_div(nkb, b.kb_per_split);
+    // stage 3: X^T Y B-ring depth
+    for (int r2 : {2, 3, max2}) {
+        if (r2 > max2 || r2 == b.ring2) continue;
+        set_rings(h, b.ring1, r2);
+        double t = 0;
+        DPCA_TRY(time_runs(h, reps, run_xty, &t));
+        if (t < best * 0.98) best = t, b.ring2 = r2;
+    }
+    set_rings(h, b.ring1, b.ring2);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[tune_class(h)] = b;
+    }
+    char buf[512];
+    snprintf(buf, sizeof(buf),
+             "{\"x_omega_ms\": [%.4f, %.4f], \"x_omega_cluster\": %d, \"ring1\": %d, \"xt_y_ms\": [%.4f, %.4f], "
+             "\"cluster\": %d, \"persistent\": %d, \"kb_per_split\": %d, \"splits\": %d, \"ring2\": %d}",
+             def_xw, best_xw, b.xw_cl, b.ring1, def_xty, best, b.xty_cl, b.xty_persistent, b.kb_per_split, m->splits,
+             b.ring2);
+    *report = buf;
+    return DPCA_OK;
+}
+
 }  // namespace dpca
+
+extern "C" dpca_status dpca_autotune(dpca_handle *hh, char *report, size_t report_cap) {
+    using namespace dpca;
+    clear_error();
+    if (!hh) return DPCA_ERR_INVALID;
+    Handle *h = &hh->h;
+    DPCA_CUDA(cudaSetDevice(h->device));
+    std::string rep;
+    dpca_status st = autotune_impl(h, &rep);
+    if (report && report_cap) {
+        strncpy(report, rep.c_str(), report_cap - 1);
+        report[report_cap - 1] = 0;
+    }
+    if (st == DPCA_OK) st = check_device_flag(h);
+    return st;
+}

@@ -212,6 +212,15 @@ dpca_status dpca_synchronize(dpca_handle *h);
 dpca_status dpca_kernel_times(dpca_handle *h, char *names, size_t names_cap, double *ms, int64_t *launches,
                               int *count, int cap);
 dpca_status dpca_reset_kernel_times(dpca_handle *h, int enable);
+/* Autotuner of the mixed-precision product kernels (no counterpart in the reference, whose
+ * products are MKL calls): measures, on this handle's resident matrix and current Omega, the
+ * cluster width of both products (CTAs sharing each dense-operand stage by multicast), X^T Y's
+ * grid mode (persistent or one CTA per work item) and K-split count, and both ring depths, one
+ * choice after another, with CUDA events; keeps the fastest for this handle and remembers it for
+ * the handle's shape class (individual tiles, SNP blocks and padded nrhs, one octave per class),
+ * which handles created later in the process start from.  report (may be NULL) gets a JSON
+ * object with the default and tuned times in ms and the choices. */
+dpca_status dpca_autotune(dpca_handle *h, char *report, size_t report_cap);
 
 /* ---- test hook: device-side failure detection without a GPU fault ----
  * Every barrier wait in the product kernels is bounded; when one runs out the kernel records the

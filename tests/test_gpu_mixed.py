@@ -158,3 +158,34 @@ def test_mixed_width_limit(dpca):
     with pytest.raises(dpca.DpcaError) as e:
         dpca.Handle(1000, 1000, 49, precision="mixed")
     assert e.value.status == 6
+
+
+def test_autotune_keeps_results(dpca):
+    """The autotuner only changes launch parameters (cluster widths, grid mode, K splits, ring
+    depths): the pass result after tuning agrees with the default one within 1e-12 (a different
+    K-split count regroups the exact partial sums in FP64), and a handle created afterwards for
+    the same shape class starts from the tuned choice and agrees as well."""
+    from distpca_gb300 import synth
+
+    n_ind, n_snp, k = 3000, 40_000, 20
+    c = synth.make_cohort(n_ind, n_snp, n_pop=4, fst=0.05, missing=0.02, seed=31)
+    packed = synth.pack_rows(c)
+    om = np.random.default_rng(3).standard_normal((n_ind, k))
+    with dpca.Handle(n_ind, n_snp, k, precision="mixed") as h:
+        h.upload(packed)
+        h.set_omega(om)
+        h.pass_()
+        z0 = h.z()
+        rep = h.autotune()
+        h.set_omega(om)
+        h.pass_()
+        z1 = h.z()
+    for key in ("x_omega_ms", "xt_y_ms", "cluster", "persistent", "kb_per_split", "ring1", "ring2", "x_omega_cluster"):
+        assert key in rep
+    assert rep["cluster"] in (0, 1, 2, 4) and rep["xt_y_ms"][1] <= rep["xt_y_ms"][0] * 1.05
+    assert np.max(np.abs(z1 - z0)) / np.max(np.abs(z0)) < 1e-12
+    with dpca.Handle(n_ind, n_snp, k, precision="mixed") as h:
+        h.upload(packed)
+        h.set_omega(om)
+        h.pass_()
+        assert np.max(np.abs(h.z() - z0)) / np.max(np.abs(z0)) < 1e-12
