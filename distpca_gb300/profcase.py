@@ -1,0 +1,98 @@
+"""Small cases of each kernel family, sized for one ncu capture, and a per-kernel breakdown of solves.
+
+    python -m distpca_gb300.profcase incore     20,000 x 100,000 (0.5 GB packed, above L2 once
+                                                transposed and split), nrhs 40, mixed: per-SNP
+                                                statistics and the transpose at upload, two passes
+                                                (X Omega, X^T Y), then a two-iteration solve
+                                                (Cholesky QR, Jacobi eigensolver, criterion)
+    python -m distpca_gb300.profcase windows    256 windows over 2,000 individuals, nrhs 8: the
+                                                batched windows' passes, QR and Rayleigh-Ritz kernels
+    python -m distpca_gb300.profcase breakdown  per-kernel device time (the handle's kernel clock)
+                                                of whole converged solves: the 1,000 x 100,000
+                                                cohort (nsv 10, nrhs 20, power 4, tol 1e-6) and
+                                                two serving-size jobs, mixed and FP64
+
+Each case holds well under 1 GB on the device and launches each kernel a handful of times, so that
+an ncu capture of one launch (`-k <kernel> -c 1`) ends by itself in a minute or two.
+"""
+from __future__ import annotations
+
+import json
+import sys
+import time
+
+import numpy as np
+
+from . import api as D
+from . import synth
+
+
+def incore() -> None:
+    n_ind, n_snp, k = 20000, 100000, 40
+    c = synth.config_cohort("incore50k", n_snp=n_snp, n_ind=n_ind)
+    with D.Handle(n_ind, n_snp, k, precision="mixed") as h:
+        h.synth_fill(c)
+        om = D.start_block(n_ind, k)
+        h.set_omega(om)
+        h.pass_()
+        h.pass_()
+        h.synchronize()
+        r = h.solve(om, nsv=20, power=2, crit=1, tol=-1, miter=2, bsize=10000)
+    print("incore ok, iterations", r["its"])
+
+
+def windows() -> None:
+    widths = synth.window_widths(256, seed=0)
+    cw = synth.make_cohort(2000, int(widths.sum()), n_pop=4, fst=0.05, missing=0.01, seed=4)
+    with D.Windows(2000, widths, 8) as w:
+        w.synth_fill(cw)
+        w.solve(nsv=2, power=3, miter=2, want_u=False)
+    print("windows ok")
+
+
+BREAKDOWN = [
+    # name, n_ind, n_snp, nrhs, nsv, power, tol, bsize, cohort
+    ("1k_x_100k", 1000, 100000, 20, 10, 4, 1e-6, 10000,
+     dict(n_pop=5, pop_sizes=[200] * 5, fst=0.05, p_range=(0.05, 0.5), missing=0.01, seed=0)),
+    ("job_4765_x_134387", 4765, 134387, 40, 20, 4, 1e-3, 134387, dict(n_pop=4, fst=0.05, missing=0.01, seed=3)),
+    ("job_2813_x_37351", 2813, 37351, 10, 5, 4, 1e-3, 37351, dict(n_pop=3, fst=0.05, missing=0.01, seed=4)),
+]
+
+
+def breakdown() -> None:
+    for name, n, m, k, nsv, power, tol, bsize, ckw in BREAKDOWN:
+        c = synth.make_cohort(n, m, **ckw)
+        for prec in ("mixed", "fp64"):
+            with D.Handle(n, m, k, precision=prec) as h:
+                h.synth_fill(c)
+                om = D.start_block(n, k)
+                h.solve(om, nsv=nsv, power=power, crit=1, tol=tol, miter=2, bsize=bsize)
+                h.reset_kernel_times(True)
+                t0 = time.perf_counter()
+                r = h.solve(om, nsv=nsv, power=power, crit=1, tol=tol, miter=100, bsize=bsize)
+                wall = time.perf_counter() - t0
+                kt = h.kernel_times()
+            tot = sum(v["ms"] for v in kt.values())
+            per = {a: [round(v["ms"], 3), v["launches"]] for a, v in sorted(kt.items(), key=lambda x: -x[1]["ms"])}
+            print(json.dumps({"case": name, "precision": prec, "its": r["its"], "wall_ms": round(wall * 1e3, 2),
+                              "kernel_ms_total": round(tot, 2), "per_kernel_ms_launches": per}), flush=True)
+
+
+CASES = {"incore": incore, "windows": windows, "breakdown": breakdown}
+
+
+def main(argv=None) -> int:
+    argv = sys.argv[1:] if argv is None else argv
+    names = argv or ["incore", "windows"]
+    for a in names:
+        if a not in CASES:
+            print(f"unknown case {a!r}; cases: {', '.join(CASES)}", file=sys.stderr)
+            return 2
+    np.set_printoptions(precision=4)
+    for a in names:
+        CASES[a]()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
