@@ -284,10 +284,14 @@ def dpca_arm(a, ranks: Ranks) -> None:
         roof = {"kernel": dom, "bound": "tensor", "achieved": flops / avg_s / 1e12,
                 "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
                 "peak_source": f"{pk['source']} bf16 sustained (kernel timed inside a multi-pass loop)"}
-        # the exact integer scheme issues two FP16 slices of the dense operand (N = 2 kp) for
-        # each of the G' and M products: 4 x kp / k times the algorithmic MMA work
+        # the exact integer scheme issues two FP16 slices of the dense operand (N = 2 kp) for the
+        # G' product (and, in the two-product kernel, again for the M product): 2 x kp / k (4 x)
+        # times the algorithmic MMA work
+        kern = (tune or {}).get("kernel") or ("gprod" if os.environ.get("DPCA_MIXED_KERNEL") == "gprod"
+                                             else "products")
         kp = (a.nrhs + 7) // 8 * 8
-        issued = flops * 4 * kp / a.nrhs
+        issued = flops * (4 if kern == "products" else 2) * kp / a.nrhs
+        roof["mixed_kernel"] = kern
         roof["issued_tensor_flop_per_launch"] = issued
         roof["frac_issued"] = issued / avg_s / 1e12 / roof["peak"]
     else:

@@ -22,7 +22,7 @@ LIB = os.path.join(OUT, "libdpca.so")
 CLI = os.path.join(OUT, "dpca")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["k_stats.cu", "k_fp64.cu", "k_dense.cu", "k_mixed.cu", "k_fullsvd.cu", "k_windows.cu", "handle.cu"]
+CU_SOURCES = ["k_stats.cu", "k_fp64.cu", "k_dense.cu", "k_mixed.cu", "k_gprod.cu", "k_fullsvd.cu", "k_windows.cu", "handle.cu"]
 CPP_SOURCES = ["host.cpp", "serve.cpp", "eig_host.cpp", "rows.cpp"]
 
 

@@ -23,8 +23,8 @@
 //   - the f2 and f1 products have one TMEM accumulator each; an accumulator sums a bounded
 //     number of K-blocks (a chunk) so that every partial sum stays within 2^24, then the drain
 //     warps copy it to registers, release it, and fold the exact integer 4096 h + l into 64-bit
-//     integer accumulators in shared memory.  The f1 chunks end half a chunk later than the f2
-//     chunks, so the tensor core keeps working on one product while the other is drained.
+//     integer accumulators in shared memory.  The f1 chunk boundaries sit half a chunk away from
+//     the f2 ones, so the tensor core keeps working on one product while the other is drained.
 // The per-SNP coefficients and the scale removal are applied once per output, in FP64.  The
 // X Omega epilogue writes Y (FP32, transposed) and the exact column maxima of |a.Y|, |(b-a).Y|,
 // from which a split kernel quantises the X^T Y operand.
@@ -52,79 +52,9 @@
 // Barriers per batch: one "full" (TMA bytes + the decode group) and one "free" (both issuers'
 // commits), so each issuer waits once and commits once per batch.  Every wait is bounded
 // (tc.cuh) and reports through h->dflag.
-#include <cuda_fp16.h>
-
-#include <algorithm>
-#include <cmath>
-#include <cstring>
-#include <map>
-#include <mutex>
-#include <string>
-#include <tuple>
-#include <vector>
-
-#include "common.cuh"
-#include "dpca_internal.h"
-#include "tc.cuh"
+#include "mixed.cuh"
 
 namespace dpca {
-
-constexpr int kXW = 1;   // Y = X Omega (rows = SNPs, K = individuals)
-constexpr int kXTY = 2;  // Z = X^T Y   (rows = individuals, K = SNPs)
-constexpr int kWarps = 15;
-constexpr int kIssuerWarpM = 14;
-constexpr int kThreads = 32 * kWarps;
-constexpr int kDecodeGroups = 2;         // one TMEM A stage per group
-constexpr int kAStages = 2;              // TMEM A stages (batch parity)
-constexpr int kPStages = 3;
-constexpr int kPStageBytes = 128 * 128;  // 128 rows x 128 B = 512 K-elements = 8 K-blocks = 4 batches
-constexpr int kTmemCols = 512;
-constexpr int kSmemFloor = 120 * 1024;   // keeps one CTA per SM (the CTA owns all of TMEM)
-constexpr int kSmemBudget = 220 * 1024;
-// Batches per exact accumulation chunk.  A batch is 8 K steps of 16 products; an f1 or f2
-// product term is at most 2 * 2048 in magnitude, so a batch adds at most 2^19 and 32 batches at
-// most 2^24.  Every partial sum is then an integer of magnitude <= 2^24, which the FP32
-// accumulator holds exactly whatever the summation order.
-constexpr int kChunkG = 32;              // f2 (= g') accumulator
-constexpr int kChunkM = 32;              // f1 accumulator
-constexpr int kFirstChunkM = 48;         // staggers the f1 drains against the f2 drains
-constexpr int kMaxMixedNrhs = 48;        // accumulators 2 x N <= 192 columns + 2 A stages of 128
-
-struct GemmArgs {
-    int rows;          // valid output rows
-    int nkb_total;     // 64-element K blocks covering K
-    int kb_per_split;  // K blocks per CTA (multiple of 8)
-    int k, kp, N;
-    int ring;          // batches in flight (B stages in shared memory)
-    int a_ktiles;      // kXTY: 128-byte K tiles per 128-row tile of the tile-blocked A operand
-    const double *coef;     // kXW: [rows][2] {b, a}
-    const double *scales;   // [4][k]: omega scale, its inverse, b/aY scale, its inverse
-    float *yt;              // kXW: Y transposed, [k][yt_ld] (FP32)
-    int64_t yt_ld;
-    unsigned int *colmax;   // kXW: per column, bits of max(|a.Y|, |(b-a).Y|) (non-negative float)
-    const long long *colsumq;  // kXW: per column, sum over individuals of the quantised Omega
-    double *y_out;          // kXW: optional FP64 Y [rows][k]
-    double *partial;        // kXTY: [splits][rows][k]
-    int *err;
-    // Batched windows (independent problems over consecutive SNP ranges, each padded to whole
-    // 512-SNP K tiles): kXW reads the window of each 128-row tile from tile_win and its Omega
-    // slices from rows [w N, w N + N) of the B map; kXTY runs one K range per blockIdx.y
-    // (win_kb0/win_nkb) and writes partial[w].  scales, colmax and colsumq then hold one block
-    // per window ([4][k], [k], [k]); CTAs of windows whose win_active entry is 0 return at once.
-    const int *tile_win;
-    const int *win_kb0, *win_nkb;
-    const int *win_active;
-    int tiles, items;  // work items = tiles x splits (tile fastest); the grid is one CTA per SM at most
-    // Limit of every barrier wait, in cycles (normally ~4 s).  A test shortens it together with
-    // `inject` = 1, which makes CTA 0's load producer withhold its first batch: the MMA issuer's
-    // wait for that batch then runs out, the kernel reports DPCA_ERR_TIMEOUT and exits cleanly.
-    long long wait_cycles = tc::kWaitCycles;
-    int inject = 0;
-};
-
-// How long a role waits, on the way out after an error, for asynchronous work it started (TMA
-// copies, MMAs) to finish: far longer than either takes.
-constexpr long long kExitCycles = 4000000;
 
 struct Handle;
 struct GemmArgs;
@@ -132,179 +62,6 @@ static int default_xty_cluster(const Handle *h);
 static void apply_tuned(Handle *h);
 static dpca_status launch_xw(Handle *h, const CUtensorMap &map_a, const CUtensorMap &map_b,
                              const CUtensorMap &map_b_band, GemmArgs a);
-
-struct MixedState {
-    int kp = 0, N = 0;
-    __half *omega_s = nullptr;  // [N][n_ind_pad]
-    __half *bop = nullptr;      // [2N][n_snp_pad]
-    float *yt = nullptr;        // [k][n_snp_pad]
-    unsigned int *colmax = nullptr;  // [k]
-    long long *colsumq = nullptr;    // [k] sum of the quantised Omega column (integers)
-    long long *rq = nullptr;         // [k] sum over SNPs of the quantised a.Y column (integers)
-    double *scales = nullptr;   // [4][k]
-    double *partial = nullptr;  // [splits][n_ind][k]
-    int splits = 1, kb_per_split = 8;
-    int ring1 = 2, ring2 = 2;
-    size_t smem1 = 0, smem2 = 0;
-    int splits_cap = 1;          // partial buffer capacity (splits)
-    int xty_cl = 0;              // X^T Y cluster width (1, 2 or 4: the dense operand is multicast; 0: by item length)
-    int xty_persistent = -1;     // X^T Y grid: 1 persistent, 0 one CTA per item, -1 by item length
-    int max_clusters[3] = {0, 0, 0};  // co-resident X^T Y clusters of width 1, 2, 4 (0: not queried)
-    CUtensorMap map_p[2], map_pt[2], map_om, map_bop;  // [1]: second block buffer when streaming
-    CUtensorMap map_bop_band[2];  // map_bop with one K-block, 2N/2 and 2N/4 rows per box (clusters of 2 and 4)
-    CUtensorMap map_om_band;      // map_om with one K-block and N/2 rows per box (X Omega in pairs)
-    int xw_cl = 0;                // X Omega cluster width (1 or 2; 0: by tile count)
-    int xw_max_clusters = 0;      // co-resident X Omega pairs (0: not queried)
-};
-
-// ------------------------------------------------------------------ decode
-// K order inside every 16-element group.  Pair register p of a 32-bit word of 16 codes holds
-// code p in its low half and code p + 8 in its high half (16 bits apart, so one mask picks both).
-// The dense operands are stored in the same order: logical K position L of a group holds element
-// perm16(L) of that group.
-__host__ __device__ __forceinline__ int perm16(int L) { return (L >> 1) + 8 * (L & 1); }
-
-__device__ __forceinline__ uint32_t fma_f16x2(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t d;
-    asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
-
-__device__ __forceinline__ uint32_t fma_relu_f16x2(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t d;
-    asm("fma.rn.relu.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
-
-// 16 packed bytes = 64 codes -> FP16 pairs: M[8q + p] holds f1 of the codes (p, p + 8) of word q,
-// G[8q + p] = relu(f1) = g'.
-//   f1: 00 -> 0, 01 (missing) -> -1, 10 -> 1, 11 -> 2;  t = f1 + 1 = c ^ (~c_hi & 1) in {1, 0, 2, 3}
-// One 3-input logic op turns a word of 16 codes c into 16 fields t.  A field at bit offset o (even,
-// o <= 8) of a 16-bit half, ORed into 0x6400 (FP16 1024, whose ulp is 1), is the FP16 value
-// 1024 + t 2^o; one FP16 FMA by 2^-o, minus (1024 2^-o + 1), gives t - 1 = f1 exactly (every
-// intermediate is a small integer or an exact power-of-two multiple).  Codes 0-4 and 8-12 sit at
-// offsets 0-8 of the word's halves; codes 5-7 and 13-15 at offsets 4-8 of the word shifted by 6.
-// So a pair costs one logic op plus two FP16 FMAs (f1, and relu(f1) for g'): the integer pipe,
-// which the byte-table decode loaded with a shift, a mask and a byte permute per pair, is the
-// busier one beside the tensor core.
-__device__ __forceinline__ void decode64(uint4 v, uint32_t (&G)[32], uint32_t (&M)[32]) {
-    // FP16 pairs {2^-o, 2^-o} and {-(1024 2^-o + 1), same} for o = 0, 2, 4, 6, 8
-    const uint32_t kScale[5] = {0x3C003C00u, 0x34003400u, 0x2C002C00u, 0x24002400u, 0x1C001C00u};
-    const uint32_t kBias[5] = {0xE401E401u, 0xDC04DC04u, 0xD410D410u, 0xCC40CC40u, 0xC500C500u};
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const uint32_t x = w[q];
-        const uint32_t t = x ^ (~(x >> 1) & 0x55555555u);
-        const uint32_t t6 = t >> 6;
-#pragma unroll
-        for (int p = 0; p < 8; ++p) {
-            const int o = p < 5 ? 2 * p : 2 * (p - 3);  // field offset inside each half
-            const uint32_t src = p < 5 ? t : t6;
-            const uint32_t h = (src & (0x00030003u << o)) | 0x64006400u;
-            M[q * 8 + p] = fma_f16x2(h, kScale[o >> 1], kBias[o >> 1]);
-            G[q * 8 + p] = fma_relu_f16x2(h, kScale[o >> 1], kBias[o >> 1]);
-        }
-    }
-}
-
-// v (already scaled, |v| < 2^23) -> nearest integer n = 4096 h + l, h and l in [-2048, 2048].
-__device__ __forceinline__ void fixed_slices(double v, __half &hi, __half &lo) {
-    const double n = rint(v);
-    const double h = rint(n * (1.0 / 4096.0));
-    hi = __double2half(h);               // exact: |h| <= 2048
-    lo = __double2half(n - 4096.0 * h);  // exact: |l| <= 2048
-}
-
-// An accumulator pair (h slice, l slice) of one chunk -> the exact integer 4096 h + l.  Both halves
-// are integers below 2^24 in FP32, so the conversions are exact; the fold stays in integer
-// arithmetic (FP64 throughput is a small fraction of the integer pipes').
-__device__ __forceinline__ long long slices_int(uint32_t hbits, uint32_t lbits) {
-    return (long long)__float2int_rz(__uint_as_float(hbits)) * 4096LL +
-           (long long)__float2int_rz(__uint_as_float(lbits));
-}
-
-// Double-float arithmetic: a value hi + lo of two FP32 numbers carries ~48 bits.  The X Omega
-// epilogue combines exact 64-bit integer sums with FP64 per-SNP coefficients; GB300's FP64 pipe
-// runs at a small fraction of its FP32 rate, and ~11 FP64 operations per output element made
-// the epilogue, not the MMAs, the cost of every short-K tile (cohorts of a few thousand).  So the
-// combination is formed from error-free FP32 products (FMA) and compensated sums (Knuth's
-// TwoSum), then rounded once to FP32.  The _rn intrinsics keep the compiler from contracting them.
-struct DF {
-    float hi, lo;
-};
-
-__device__ __forceinline__ DF df_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
-}
-
-// FP64 coefficient -> hi + lo
-__device__ __forceinline__ DF df_from_double(double x) {
-    const float h = (float)x;
-    return {h, (float)(x - (double)h)};
-}
-
-// A power of two held in FP64 as FP32, by integer arithmetic on its exponent; 0 when it is not an
-// FP32 normal number (an Omega column below ~1e-31 or above ~1e45), for which the caller falls back
-// to FP64.  (Y itself is FP32, so the mixed pass serves Omega columns of about 1e-30 to 1e37; the
-// solver's Omega is orthonormal.)
-__device__ __forceinline__ float pow2_to_float(double x) {
-    const long long bits = __double_as_longlong(x);
-    const int e = (int)((bits >> 52) & 0x7FF) - 1023;
-    if (e < -126 || e > 127) return 0.f;
-    return __int_as_float((int)(bits >> 32 & 0x80000000) | ((e + 127) << 23));
-}
-
-// c * x for an exact integer x (|x| < 2^48: x = H 2^24 + L with H, L exact in FP32).
-__device__ __forceinline__ DF df_mul_int(DF c, long long x) {
-    const float xh = __fmul_rn((float)(int)(x >> 24), 16777216.f);
-    const float xl = (float)(int)(x & 0xFFFFFF);
-    const float p1 = __fmul_rn(c.hi, xh), p2 = __fmul_rn(c.hi, xl);
-    const float e1 = __fmaf_rn(c.hi, xh, -p1), e2 = __fmaf_rn(c.hi, xl, -p2);
-    const DF s = df_two_sum(p1, p2);
-    const float t = __fmaf_rn(c.lo, __fadd_rn(xh, xl), __fadd_rn(__fadd_rn(e1, e2), s.lo));
-    return df_two_sum(s.hi, t);
-}
-
-// Slow path of a wait, out of line so that the MMA issue loop stays compact (an inlined wait
-// loop in that loop costs ~90 cycles per iteration even when it never runs).
-__device__ __noinline__ bool wait_slow(uint64_t *bar, uint32_t parity, int *err, int code, long long limit) {
-    return tc::mbar_wait(bar, parity, err, code, false, limit);
-}
-
-__device__ __forceinline__ bool wait_fast(uint64_t *bar, uint32_t parity, int *err, int code, long long limit) {
-    return tc::mbar_try_wait(bar, parity) || wait_slow(bar, parity, err, code, limit);
-}
-
-// Chunks of an accumulator whose first chunk has `first` batches and the others `len`.
-__device__ __forceinline__ int chunk_count(int nb, int first, int len) {
-    return nb <= first ? 1 : 1 + (nb - first + len - 1) / len;
-}
-
-__device__ __forceinline__ int chunk_end(int c, int nb, int first, int len) {
-    return min(first - 1 + c * len, nb - 1);
-}
-
-// Work item `it` of a launch: tile it % tiles, split it / tiles (for batched windows, the window
-// of the tile or the split); nb = 0 for a window that has converged.  Every role of a CTA
-// evaluates the same items in the same order.
-struct WorkItem {
-    int tile, split, win, kb0, nb;
-};
-
-__device__ __forceinline__ WorkItem work_item(const GemmArgs &a, int it) {
-    WorkItem x;
-    x.tile = it % a.tiles;
-    x.split = it / a.tiles;
-    x.win = a.tile_win ? a.tile_win[min(x.tile, (a.rows + 127) / 128 - 1)] : (a.win_kb0 ? x.split : 0);
-    const bool skip = (a.tile_win || a.win_kb0) && a.win_active && !a.win_active[x.win];
-    x.kb0 = a.win_kb0 ? a.win_kb0[x.split] : x.split * a.kb_per_split;
-    const int nkb = a.win_kb0 ? a.win_nkb[x.split] : min(a.nkb_total, x.kb0 + a.kb_per_split) - x.kb0;
-    x.nb = skip ? 0 : (nkb + 1) >> 1;  // a trailing half batch reads zero operand columns
-    return x;
-}
 
 // CL > 1: the kernel runs in clusters of CL CTAs that walk consecutive row tiles of the same K
 // range in lockstep (X Omega: consecutive SNP tiles, which all read the same Omega slices), and
@@ -394,7 +151,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             int withheld = 0;
             const long long lim = args.wait_cycles;
             for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
-                const WorkItem x = work_item(args, it);
+                const WorkItem x = work_item(args, it, 2);
                 const int b_row0 = args.tile_win ? x.win * N : 0;  // this window's Omega slices
                 for (int t = 0; t < x.nb; ++t) {
                     if ((t & 3) == 0) {
@@ -470,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         uint32_t ph = 0, stage = 0;  // stage = global batch parity
         bool ok = true;
         for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
-            const int nb = work_item(args, it).nb;
+            const int nb = work_item(args, it, 2).nb;
             int left = first_len;
             bool fresh = true;
             for (int t = 0; t < nb; ++t) {
@@ -528,7 +285,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         int gb = 0, pgl = 0;     // global batch and packed-stage load index at the item's start
         bool ok = true;
         for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
-            const int nb = work_item(args, it).nb;
+            const int nb = work_item(args, it, 2).nb;
             const int nst = (nb + 3) >> 2;
             for (int pgi = 0; ok && pgi < nst; ++pgi) {
                 const int pg = pgl + pgi, sp = pg % kPStages;
@@ -576,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         int cgG = 0, cgM = 0;  // chunks of each accumulator drained so far (all items): barrier parity
         bool ok = true;
         for (int it = blockIdx.x; ok && it < args.items; it += gridDim.x) {
-            const WorkItem x = work_item(args, it);
+            const WorkItem x = work_item(args, it, 2);
             const int nb = x.nb;
             if (nb == 0) continue;
             const int row = x.tile * 128 + r;
@@ -696,15 +453,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 1) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
-// ------------------------------------------------------------------ operand preparation
-__device__ __forceinline__ double pow2_scale_below(double bound) {
-    // largest power of two s with bound * s < 2^23 (1 when bound is 0 or not finite)
-    if (!(bound > 0.0) || !isfinite(bound)) return 1.0;
-    int e;
-    frexp(bound, &e);  // bound < 2^e
-    return ldexp(1.0, 23 - e);
-}
-
 // Block per column c of Omega: the power-of-two scale for its fixed-point slices.
 __global__ void __launch_bounds__(256) omega_scales_kernel(const double *__restrict__ om, int n, int k,
                                                            double *__restrict__ scales) {
@@ -724,10 +472,12 @@ __global__ void __launch_bounds__(256) omega_scales_kernel(const double *__restr
 }
 
 // omega_s[c][i] = h, omega_s[kp + c][i] = l of round(Omega[src][c] * scale_c), src = the
-// individual at K position i (perm16 order inside groups of 16); zero padding elsewhere.
+// individual at K position i (perm16 order inside groups of 16); zero padding elsewhere.  With oq
+// (the G'-product kernel), also oq[src][c] = the rounded integer itself.
 __global__ void __launch_bounds__(256) omega_split_kernel(const double *__restrict__ om, int n, int k, int kp,
                                                           int n_pad, const double *__restrict__ scales,
-                                                          __half *__restrict__ out, long long *__restrict__ colsumq) {
+                                                          __half *__restrict__ out, long long *__restrict__ colsumq,
+                                                          int *__restrict__ oq) {
     const int64_t total = (int64_t)kp * n_pad;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int c = (int)(e / n_pad), i = (int)(e - (int64_t)c * n_pad);
@@ -741,6 +491,7 @@ __global__ void __launch_bounds__(256) omega_split_kernel(const double *__restri
         }
         out[(int64_t)c * n_pad + i] = hi;
         out[(int64_t)(kp + c) * n_pad + i] = lo;
+        if (oq) oq[(int64_t)src * kp + c] = q;
         // exact column sum of the quantised integers (a warp covers 32 consecutive i of one
         // column: n_pad is a multiple of 128); integer adds, so the order does not matter
         const int ws = __reduce_add_sync(0xffffffffu, q);
@@ -939,8 +690,8 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base, uint64_t inner, uint64_t outer,
-                            uint64_t row_bytes, uint32_t box_inner, uint32_t box_outer) {
+dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base, uint64_t inner, uint64_t outer,
+                     uint64_t row_bytes, uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swizzle) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) {
         set_error("cuTensorMapEncodeTiled unavailable");
@@ -950,8 +701,8 @@ static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base
     cuuint64_t strides[1] = {row_bytes};
     cuuint32_t box[2] = {box_inner, box_outer};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, dt, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = fn(map, dt, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (%d): dims %llu x %llu, box %u x %u", (int)r,
                   (unsigned long long)inner, (unsigned long long)outer, box_inner, box_outer);
@@ -964,8 +715,8 @@ static dpca_status make_map(CUtensorMap *map, CUtensorMapDataType dt, void *base
 // K-blocks, each a rows x 128 B tile (n_pad is a multiple of 128, so whole batches exist).
 // FP16 operand [rows][n_pad] as 3-D boxes of box_rows rows x 2 K-blocks of 64 (box_rows = rows,
 // or the N rows of one window when the rows stack several windows' slices).
-static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, uint64_t rows, uint32_t box_rows = 0,
-                                  uint32_t box_kblocks = 2) {
+dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, uint64_t rows, uint32_t box_rows,
+                           uint32_t box_kblocks) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) {
         set_error("cuTensorMapEncodeTiled unavailable");
@@ -986,8 +737,6 @@ static dpca_status make_batch_map(CUtensorMap *map, void *base, uint64_t n_pad, 
     return DPCA_OK;
 }
 
-static MixedState *mstate(Handle *h) { return (MixedState *)h->mx; }
-
 static size_t acc_bytes(int mode, int kp) { return (size_t)(mode == kXW ? 2 : 1) * kp * 128 * 8; }
 static size_t batch_bytes(int mode, int N) { return (size_t)2 * (mode == kXW ? 1 : 2) * N * 128; }
 static size_t fixed_bytes(int mode, int kp) {
@@ -1000,7 +749,7 @@ static size_t fixed_bytes(int mode, int kp) {
 // (tens of MB each) then no longer share L2, while the hardware scheduler keeps concurrently
 // running CTAs on neighbouring items (measured at 50,000 x 1,000,000: 19.5 ms persistent vs
 // 15.9 ms one CTA per item).  X Omega shares one L2-resident operand and is always persistent.
-static int xty_grid(Handle *h, int items, int batches_per_item) {
+int xty_grid(Handle *h, int items, int batches_per_item) {
     const int mode = h->mx ? mstate(h)->xty_persistent : -1;
     const bool per_item = mode < 0 ? batches_per_item > 128 : mode == 0;
     return per_item ? items : std::min(items, h->sm_count);
@@ -1095,6 +844,10 @@ dpca_status mixed_prepare(Handle *h) {
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 2>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 4>));
     m->xty_cl = default_xty_cluster(h);
+    // kernel: the two-product kernel unless DPCA_MIXED_KERNEL = gprod (or a tuned choice) says
+    // otherwise; windows always run the two-product kernel (its per-window operand layout)
+    if (const char *e = getenv("DPCA_MIXED_KERNEL")) m->kernel = strcmp(e, "gprod") == 0 ? 1 : 0;
+    DPCA_TRY(gprod_prepare(h));
     apply_tuned(h);
     return DPCA_OK;
 }
@@ -1109,7 +862,7 @@ size_t mixed_footprint(int n_ind, int n_snp, int nrhs, int sm_count) {
     const size_t kp = (size_t)(nrhs + 7) / 8 * 8, N = 2 * kp;
     const size_t n_pad = (size_t)(n_ind + 127) / 128 * 128, rows_pad = (size_t)(n_snp + 127) / 128 * 128;
     return N * n_pad * 2 + 2 * N * rows_pad * 2 + 4 * (size_t)nrhs * 8 + (size_t)nrhs * rows_pad * 4 +
-           (size_t)nrhs * 20 + (size_t)splits * n_ind * nrhs * 8;
+           (size_t)nrhs * 20 + (size_t)splits * n_ind * nrhs * 8 + gprod_footprint(n_ind, n_snp, nrhs);
 }
 
 dpca_status mixed_release(Handle *h) {
@@ -1117,6 +870,7 @@ dpca_status mixed_release(Handle *h) {
     if (!m) return DPCA_OK;
     void *ptrs[] = {m->omega_s, m->bop, m->yt, m->colmax, m->scales, m->partial, m->colsumq, m->rq};
     for (void *p : ptrs) dev_free(h, p);
+    gprod_release(h);
     delete m;
     h->mx = nullptr;
     return DPCA_OK;
@@ -1132,7 +886,7 @@ dpca_status mixed_omega_operand(Handle *h, const double *omega) {
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 8);
     DPCA_CUDA(cudaMemsetAsync(m->colsumq, 0, (size_t)k * 8, h->stream));
     omega_split_kernel<<<grid, 256, 0, h->stream>>>(omega, h->n_ind, k, m->kp, h->n_ind_pad, m->scales, m->omega_s,
-                                                    m->colsumq);
+                                                    m->colsumq, m->kernel == 1 ? m->omega_q : nullptr);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -1165,6 +919,14 @@ static dpca_status xw_rows(Handle *h, const CUtensorMap &map_a, int rows, const 
     }
     DPCA_CUDA(cudaMemsetAsync(m->colmax, 0, (size_t)k * 4, h->stream));
     DPCA_CUDA(cudaMemsetAsync(m->rq, 0, (size_t)k * 8, h->stream));
+    if (m->kernel == 1) {
+        {
+            ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
+            DPCA_TRY(gprod_xw(h, map_a, a));
+        }
+        ScopedLaunch t(&h->clock, h->stream, "split_bop");
+        return gprod_split_bop(h, rows, coef);
+    }
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xw");
         DPCA_TRY(launch_xw(h, map_a, m->map_om, m->map_om_band, a));
@@ -1313,7 +1075,8 @@ static dpca_status xty_rows(Handle *h, const CUtensorMap &map_a, int nsnp, doubl
     a.err = h->dflag;
     {
         ScopedLaunch t(&h->clock, h->stream, "mixed_xty");
-        DPCA_TRY(launch_xty(h, map_a, a, splits, kb_per_split / 2));
+        if (m->kernel == 1) DPCA_TRY(gprod_xty(h, map_a, a, splits, kb_per_split / 2));
+        else DPCA_TRY(launch_xty(h, map_a, a, splits, kb_per_split / 2));
     }
     ScopedLaunch t(&h->clock, h->stream, "mixed_reduce");
     int64_t elems = (int64_t)h->n_ind * k;
@@ -1426,7 +1189,10 @@ dpca_status mixed_block(Handle *h, int b, int s0, int ns, double *z, bool accumu
 }
 
 // ------------------------------------------------------------------ autotuner
-// The product kernels' launch parameters -- X^T Y's cluster width (1, 2, 4), grid mode
+// The product kernels' launch parameters -- the kernel (G' product with the missing term on the
+// CUDA cores, or the two products: the first wins on matrices with few missing genotypes, the
+// second when they are dense enough that the per-row missing sums cost more than a second
+// tensor-core product), X^T Y's cluster width (1, 2, 4), grid mode
 // (persistent or one CTA per work item), K-split count and B-ring depth, and X Omega's cluster
 // width (1, 2) and B-ring depth -- measured on a handle's own matrix, choice by choice, with CUDA
 // events on its stream, and remembered for the handle's shape class (individual tiles, SNP
@@ -1434,7 +1200,7 @@ dpca_status mixed_block(Handle *h, int b, int s0, int ns, double *z, bool accumu
 // (serving jobs, repeated solves) start from the measured choice.  The heuristics (pick_splits,
 // pick_ring, the cluster and grid rules) are what a shape class without a measurement uses.
 struct TuneChoice {
-    int xty_cl = 0, xty_persistent = -1, kb_per_split = 0, ring1 = 0, ring2 = 0, xw_cl = 0;
+    int xty_cl = 0, xty_persistent = -1, kb_per_split = 0, ring1 = 0, ring2 = 0, xw_cl = 0, kernel = -1;
 };
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int>, TuneChoice> g_tune;
@@ -1444,8 +1210,13 @@ static std::tuple<int, int, int> tune_class(const Handle *h) {
     return std::make_tuple(oct(ceil_div(h->n_ind, 128)), oct(ceil_div(h->rows_dev, 64)), (h->k + 7) / 8 * 8);
 }
 
+// Ring depths of the kernel in use (the two-product kernel's also serve the batched windows).
 static void set_rings(Handle *h, int ring1, int ring2) {
     MixedState *m = mstate(h);
+    if (m->kernel == 1) {
+        gprod_set_rings(h, ring1, ring2);
+        return;
+    }
     const int max1 = pick_ring(kXW, m->N, m->kp), max2 = pick_ring(kXTY, m->N, m->kp);
     m->ring1 = std::max(2, std::min(ring1, max1));
     m->ring2 = std::max(2, std::min(ring2, max2));
@@ -1463,6 +1234,7 @@ static void apply_tuned(Handle *h) {
         c = it->second;
     }
     MixedState *m = mstate(h);
+    if (c.kernel >= 0 && getenv("DPCA_MIXED_KERNEL") == nullptr) m->kernel = c.kernel;
     if (getenv("DPCA_XTY_CLUSTER") == nullptr) m->xty_cl = c.xty_cl;
     m->xw_cl = c.xw_cl;
     m->xty_persistent = c.xty_persistent;
@@ -1505,8 +1277,25 @@ static dpca_status autotune_impl(Handle *h, std::string *report) {
     const int reps = 2;
     auto run_xw = [&]() { return launch_mixed_xw(h, h->omega, nullptr); };
     auto run_xty = [&]() { return launch_mixed_xty(h, h->z); };
-    const int max1 = pick_ring(kXW, m->N, m->kp), max2 = pick_ring(kXTY, m->N, m->kp);
-    const TuneChoice def{m->xty_cl, m->xty_persistent, m->kb_per_split, m->ring1, m->ring2, m->xw_cl};
+    // stage 0: the kernel, on a whole pass with each kernel's default launch parameters (unless
+    // DPCA_MIXED_KERNEL fixes it)
+    auto run_pass = [&]() {
+        DPCA_TRY(run_xw());
+        return run_xty();
+    };
+    double pass_ms[2] = {0.0, 0.0};
+    if (getenv("DPCA_MIXED_KERNEL") == nullptr) {
+        for (int kk : {1, 0}) {
+            m->kernel = kk;
+            DPCA_TRY(time_runs(h, reps, run_pass, &pass_ms[kk]));
+        }
+        m->kernel = pass_ms[1] < pass_ms[0] * 0.98 ? 1 : 0;
+    }
+    const bool g = m->kernel == 1;
+    const int max1 = g ? gprod_max_ring(h) : pick_ring(kXW, m->N, m->kp);
+    const int max2 = g ? gprod_max_ring(h) : pick_ring(kXTY, m->N, m->kp);
+    const TuneChoice def{m->xty_cl,  m->xty_persistent,       m->kb_per_split, g ? m->gring1 : m->ring1,
+                         g ? m->gring2 : m->ring2, m->xw_cl, m->kernel};
     TuneChoice b = def;
     // X Omega: cluster width, then B-ring depth
     double def_xw = 0, best_xw = 0;
@@ -1523,12 +1312,12 @@ static dpca_status autotune_impl(Handle *h, std::string *report) {
     m->xw_cl = b.xw_cl;
     for (int r1 : {2, 3, max1}) {
         if (r1 > max1 || r1 == b.ring1) continue;
-        set_rings(h, r1, m->ring2);
+        set_rings(h, r1, b.ring2);
         double t = 0;
         DPCA_TRY(time_runs(h, reps, run_xw, &t));
         if (t < best_xw * 0.98) best_xw = t, b.ring1 = r1;
     }
-    set_rings(h, b.ring1, m->ring2);
+    set_rings(h, b.ring1, b.ring2);
     DPCA_TRY(run_xw());  // the Y operand for the X^T Y trials
     // X^T Y stage 1: cluster width x grid mode
     double def_xty = 0, best = 0;
@@ -1584,12 +1373,13 @@ static dpca_status autotune_impl(Handle *h, std::string *report) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[tune_class(h)] = b;
     }
-    char buf[512];
+    char buf[768];
     snprintf(buf, sizeof(buf),
-             "{\"x_omega_ms\": [%.4f, %.4f], \"x_omega_cluster\": %d, \"ring1\": %d, \"xt_y_ms\": [%.4f, %.4f], "
+             "{\"kernel\": \"%s\", \"pass_ms\": {\"gprod\": %.4f, \"products\": %.4f}, "
+             "\"x_omega_ms\": [%.4f, %.4f], \"x_omega_cluster\": %d, \"ring1\": %d, \"xt_y_ms\": [%.4f, %.4f], "
              "\"cluster\": %d, \"persistent\": %d, \"kb_per_split\": %d, \"splits\": %d, \"ring2\": %d}",
-             def_xw, best_xw, b.xw_cl, b.ring1, def_xty, best, b.xty_cl, b.xty_persistent, b.kb_per_split, m->splits,
-             b.ring2);
+             b.kernel == 1 ? "gprod" : "products", pass_ms[1], pass_ms[0], def_xw, best_xw, b.xw_cl, b.ring1, def_xty,
+             best, b.xty_cl, b.xty_persistent, b.kb_per_split, m->splits, b.ring2);
     *report = buf;
     return DPCA_OK;
 }

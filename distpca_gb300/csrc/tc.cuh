@@ -158,6 +158,16 @@ __device__ __forceinline__ void tma_load_3d_mc(void *smem_dst, const CUtensorMap
         : "memory");
 }
 
+// 2-D tile load multicast to the CTAs of this cluster in `mask` (as tma_load_3d_mc).
+__device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
+                                               uint16_t mask) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, "
+        "{%3, %4}], [%2], %5;" ::"r"(smem_u32(smem_dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "h"(mask)
+        : "memory");
+}
+
 // ------------------------------------------------------------------ clusters
 __device__ __forceinline__ uint32_t cluster_ctarank() {
     uint32_t r;

@@ -161,10 +161,12 @@ def test_mixed_width_limit(dpca):
 
 
 def test_autotune_keeps_results(dpca):
-    """The autotuner only changes launch parameters (cluster widths, grid mode, K splits, ring
-    depths): the pass result after tuning agrees with the default one within 1e-12 (a different
-    K-split count regroups the exact partial sums in FP64), and a handle created afterwards for
-    the same shape class starts from the tuned choice and agrees as well."""
+    """The autotuner changes launch parameters (cluster widths, grid mode, K splits, ring depths)
+    and may switch kernels.  With the default kernel kept, the pass result after tuning agrees
+    with the default one within 1e-12 (a different K-split count regroups the exact partial sums in
+    FP64); after a switch to the G'-product kernel, within that kernel's tolerance (3e-6: X^T Y
+    rounds different products to fixed point).  A handle created afterwards for the same shape
+    class starts from the tuned choice and agrees with the tuned result within 1e-12."""
     from distpca_gb300 import synth
 
     n_ind, n_snp, k = 3000, 40_000, 20
@@ -183,9 +185,11 @@ def test_autotune_keeps_results(dpca):
     for key in ("x_omega_ms", "xt_y_ms", "cluster", "persistent", "kb_per_split", "ring1", "ring2", "x_omega_cluster"):
         assert key in rep
     assert rep["cluster"] in (0, 1, 2, 4) and rep["xt_y_ms"][1] <= rep["xt_y_ms"][0] * 1.05
-    assert np.max(np.abs(z1 - z0)) / np.max(np.abs(z0)) < 1e-12
+    assert rep["kernel"] in ("gprod", "products")
+    tol = 1e-12 if rep["kernel"] == "products" else 3e-6
+    assert np.max(np.abs(z1 - z0)) / np.max(np.abs(z0)) < tol
     with dpca.Handle(n_ind, n_snp, k, precision="mixed") as h:
         h.upload(packed)
         h.set_omega(om)
         h.pass_()
-        assert np.max(np.abs(h.z() - z0)) / np.max(np.abs(z0)) < 1e-12
+        assert np.max(np.abs(h.z() - z1)) / np.max(np.abs(z1)) < 1e-12
