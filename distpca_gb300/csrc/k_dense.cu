@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const double *__re
     double *V = k <= kEigSmemK ? esm + k * k : vglobal;
     const int tid = threadIdx.x, kk2 = k * k;
     const int kk = k + (k & 1), npairs = kk / 2;
+    const int i0 = tid / k, j0 = tid - i0 * k, di = kEigThreads / k, dj = kEigThreads - di * k;
     const double eps = 0x1p-52;
     for (int e = tid; e < kk2; e += kEigThreads) {
         const int i = e / k, j = e - i * k;
@@ -187,31 +188,42 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const double *__re
                 sn[tid] = s;
             }
             __syncthreads();
-            // step 2: rows p, q of A for every pair (pairs touch disjoint rows)
-            for (int e = tid; e < npairs * k; e += kEigThreads) {
-                const int i = e / k, j = e - i * k;
+            // step 2: rows p, q of A for every pair (pairs touch disjoint rows).  Element e = (pair
+            // i, column j) of the npairs x k grid, e = tid, tid + 256, ...: (i, j) advance by
+            // (di, dj) with a carry, and every lane of a warp has work (the FP64 pipe runs a warp
+            // instruction for all its lanes).  The solve's time is the FP64 rotations' dependent
+            // chains and the three barriers per round, not this indexing (measured: unchanged
+            // from a per-element division).
+            for (int i = i0, j = j0; i < npairs;) {
                 const double s = sn[i];
-                if (s == 0.0) continue;
-                const double c = cs[i];
-                const int p = pp[i], q = qq[i];
-                const double ap = A[p * k + j], aq = A[q * k + j];
-                A[p * k + j] = c * ap - s * aq;
-                A[q * k + j] = s * ap + c * aq;
+                if (s != 0.0) {
+                    const double c = cs[i];
+                    const int p = pp[i], q = qq[i];
+                    const double ap = A[p * k + j], aq = A[q * k + j];
+                    A[p * k + j] = c * ap - s * aq;
+                    A[q * k + j] = s * ap + c * aq;
+                }
+                i += di;
+                j += dj;
+                if (j >= k) j -= k, ++i;
             }
             __syncthreads();
             // step 3: columns p, q of A and V; the annihilated pair is set to zero exactly
-            for (int e = tid; e < npairs * k; e += kEigThreads) {
-                const int i = e / k, j = e - i * k;
+            for (int i = i0, j = j0; i < npairs;) {
                 const double s = sn[i];
-                if (s == 0.0) continue;
-                const double c = cs[i];
-                const int p = pp[i], q = qq[i];
-                const double ap = A[j * k + p], aq = A[j * k + q];
-                A[j * k + p] = j == q ? 0.0 : c * ap - s * aq;
-                A[j * k + q] = j == p ? 0.0 : s * ap + c * aq;
-                const double vp = V[j * k + p], vq = V[j * k + q];
-                V[j * k + p] = c * vp - s * vq;
-                V[j * k + q] = s * vp + c * vq;
+                if (s != 0.0) {
+                    const double c = cs[i];
+                    const int p = pp[i], q = qq[i];
+                    const double ap = A[j * k + p], aq = A[j * k + q];
+                    A[j * k + p] = j == q ? 0.0 : c * ap - s * aq;
+                    A[j * k + q] = j == p ? 0.0 : s * ap + c * aq;
+                    const double vp = V[j * k + p], vq = V[j * k + q];
+                    V[j * k + p] = c * vp - s * vq;
+                    V[j * k + q] = s * vp + c * vq;
+                }
+                i += di;
+                j += dj;
+                if (j >= k) j -= k, ++i;
             }
             __syncthreads();
         }
@@ -324,10 +336,10 @@ __global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__
             const double inv = pinv[j];
             for (int c = j + 1 + tid; c < k; c += kCholThreads) S[j * k + c] *= inv;
             __syncthreads();
-            const int m = k - j - 1;
-            for (int e = tid; e < m * m; e += kCholThreads) {
-                const int a = j + 1 + e / m, c = j + 1 + e % m;
-                if (c >= a) S[a * k + c] -= S[j * k + a] * S[j * k + c];
+            // trailing upper triangle: a warp per row, its lanes over the row's columns
+            for (int a = j + 1 + (tid >> 5); a < k; a += kCholThreads / 32) {
+                const double sa = S[j * k + a];
+                for (int c = a + (tid & 31); c < k; c += 32) S[a * k + c] -= sa * S[j * k + c];
             }
             __syncthreads();
         }
