@@ -247,17 +247,241 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const double *__re
     }
 }
 
+// The same Jacobi solve with the rotations applied in double-float arithmetic: every entry of A
+// and V is a pair of FP32 numbers hi + lo (~47 bits), each update c a - s b is formed from
+// error-free FP32 products (FMA) and compensated sums.  GB300 runs FP32 at many times its FP64
+// rate, and the row and column updates -- ~5 k^2 FMAs per round, all of the solve's arithmetic --
+// bound the FP64 kernel on its one SM together with the rotations' dependent FP64 division and
+// square-root chains (a warp's FP64 instruction occupies the narrow FP64 pipe for many cycles).
+// The rotations are formed in double-float too: an FP32 root or quotient and one compensated
+// correction each.  The relative skip test uses 2^-44 in place of FP64's epsilon, with an absolute
+// floor of 2^-47, so the sweeps end at the pairs' precision.  B is scaled by a power of two to
+// max |b| in [1/2, 1) first (FP32's exponent range), and the eigenvalues scaled back exactly.
+// Each rotation's c^2 + s^2 is 1 within ~2^-46, and that error compounds over the ~2k rotations an
+// entry takes per sweep: eigenvalues and eigenvectors come out within 1e-12 of max |w| up to k = 48
+// (checked against LAPACK in the tests, as the FP64 kernel), ~2e-12 at k = 97.  So this kernel
+// serves k <= kEigDfMaxK -- every mixed-precision width and the usual nrhs -- and the FP64 kernel
+// the rest.
+struct DFp {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DFp dfp_of(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
+__device__ __forceinline__ double dfp_val(DFp a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ DFp dfp_fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// c x + d y for pairs c, x, d, y (d = -s or s): two error-free products, one compensated sum
+__device__ __forceinline__ DFp dfp_dot2(DFp c, DFp x, DFp d, DFp y) {
+    const float p1 = __fmul_rn(c.hi, x.hi), p2 = __fmul_rn(d.hi, y.hi);
+    float e1 = __fmaf_rn(c.hi, x.hi, -p1), e2 = __fmaf_rn(d.hi, y.hi, -p2);
+    e1 = __fmaf_rn(c.hi, x.lo, __fmaf_rn(c.lo, x.hi, e1));
+    e2 = __fmaf_rn(d.hi, y.lo, __fmaf_rn(d.lo, y.hi, e2));
+    const float sh = __fadd_rn(p1, p2);  // two_sum(p1, p2)
+    const float bb = __fsub_rn(sh, p1);
+    const float sl = __fadd_rn(__fsub_rn(p1, __fsub_rn(sh, bb)), __fsub_rn(p2, bb));
+    return dfp_fast_two_sum(sh, __fadd_rn(sl, __fadd_rn(e1, e2)));
+}
+
+__device__ __forceinline__ DFp dfp_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+__device__ __forceinline__ DFp dfp_add(DFp a, DFp b) {
+    const DFp t = dfp_two_sum(a.hi, b.hi);
+    return dfp_fast_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ DFp dfp_mul(DFp a, DFp b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p)));
+    return dfp_fast_two_sum(p, e);
+}
+
+// a / b: an FP32 quotient and one correction from the exact-ish remainder a - q b
+__device__ __forceinline__ DFp dfp_div(DFp a, DFp b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const DFp r = dfp_add(a, dfp_mul(b, DFp{-q1, 0.f}));
+    return dfp_fast_two_sum(q1, __fdiv_rn(r.hi, b.hi));
+}
+
+// sqrt(a), a >= 0: the correctly rounded FP32 root x and one Newton correction (a - x^2) / 2x
+__device__ __forceinline__ DFp dfp_sqrt(DFp a) {
+    if (!(a.hi > 0.f)) return DFp{0.f, 0.f};
+    const float x = __fsqrt_rn(a.hi);
+    const float p = __fmul_rn(x, x), pe = __fmaf_rn(x, x, -p);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), a.lo);
+    return dfp_fast_two_sum(x, __fdiv_rn(r, __fmul_rn(2.f, x)));
+}
+
+__global__ void __launch_bounds__(kEigThreads) sym_eig_df_kernel(const double *__restrict__ Bin, int k,
+                                                                 double *__restrict__ Wout, double *__restrict__ wout,
+                                                                 int *__restrict__ err) {
+    extern __shared__ DFp dsm[];  // A | V, k x k pairs each
+    __shared__ DFp cs[64], sn[64];
+    __shared__ double dg[128], red[kEigThreads / 32];
+    __shared__ int pp[64], qq[64], ord[128];
+    __shared__ int rotated;
+    __shared__ double scale;
+    DFp *A = dsm, *V = dsm + k * k;
+    const int tid = threadIdx.x, kk2 = k * k;
+    const int kk = k + (k & 1), npairs = kk / 2;
+    const int i0 = tid / k, j0 = tid - i0 * k, di = kEigThreads / k, dj = kEigThreads - di * k;
+    const double eps = 0x1p-44;
+    // power-of-two scale: max |b| of the upper triangle into [1/2, 1)
+    double mx = 0.0;
+    for (int e = tid; e < kk2; e += kEigThreads) {
+        const int i = e / k, j = e - i * k;
+        if (i <= j) mx = fmax(mx, fabs(Bin[e]));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) red[tid >> 5] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        double m = 0.0;
+        for (int w = 0; w < kEigThreads / 32; ++w) m = fmax(m, red[w]);
+        int ex = 0;
+        if (m > 0.0 && isfinite(m)) frexp(m, &ex);
+        scale = ldexp(1.0, -ex);
+    }
+    __syncthreads();
+    const double sc = scale;
+    for (int e = tid; e < kk2; e += kEigThreads) {
+        const int i = e / k, j = e - i * k;
+        A[e] = dfp_of((i <= j ? Bin[e] : Bin[j * k + i]) * sc);
+        V[e] = DFp{i == j ? 1.f : 0.f, 0.f};
+    }
+    __syncthreads();
+    int sweep = 0;
+    for (; sweep < kEigMaxSweeps && k > 1; ++sweep) {
+        if (tid == 0) rotated = 0;
+        __syncthreads();
+        for (int r = 0; r < kk - 1; ++r) {
+            if (tid < npairs) {
+                int p = tid == 0 ? 0 : 1 + (r + tid) % (kk - 1);
+                int q = tid == 0 ? 1 + r % (kk - 1) : 1 + (r - tid + kk - 1) % (kk - 1);
+                if (p > q) {
+                    const int t = p;
+                    p = q;
+                    q = t;
+                }
+                DFp c = {1.f, 0.f}, s = {0.f, 0.f};
+                if (q < k) {
+                    const DFp apq = A[p * k + q], app = A[p * k + p], aqq = A[q * k + q];
+                    // the skip test on the leading parts; also an absolute floor at the pairs'
+                    // rounding level (max |a| < 1 after the scaling), so that the sweeps end when a
+                    // diagonal entry is ~0
+                    if (fabsf(apq.hi) > fmaxf(0.5f * (float)eps * sqrtf(fabsf(app.hi * aqq.hi)), 0x1p-47f)) {
+                        // t = tan of the angle that zeroes a_pq, in the form without cancellation:
+                        // sgn(theta) 2 |a_pq| / (|d| + sqrt(d^2 + 4 a_pq^2)), d = a_qq - a_pp,
+                        // theta = d / (2 a_pq) (theta = 0 takes the + sign); then
+                        // c = 1 / sqrt(1 + t^2), s = t c -- all in double-float
+                        const DFp d = dfp_add(aqq, DFp{-app.hi, -app.lo});
+                        const bool neg = (d.hi < 0.f) != (apq.hi < 0.f) && d.hi != 0.f;
+                        const DFp ad = d.hi < 0.f ? DFp{-d.hi, -d.lo} : d;
+                        const DFp aa = apq.hi < 0.f ? DFp{-apq.hi, -apq.lo} : apq;
+                        const DFp two_a = {2.f * aa.hi, 2.f * aa.lo};
+                        const DFp rt = dfp_sqrt(dfp_add(dfp_mul(ad, ad), dfp_mul(two_a, two_a)));
+                        DFp t = dfp_div(two_a, dfp_add(ad, rt));
+                        if (neg) t = DFp{-t.hi, -t.lo};
+                        c = dfp_div(DFp{1.f, 0.f}, dfp_sqrt(dfp_add(DFp{1.f, 0.f}, dfp_mul(t, t))));
+                        s = dfp_mul(t, c);
+                        if (s.hi != 0.f) rotated = 1;
+                    }
+                }
+                pp[tid] = p;
+                qq[tid] = q;
+                cs[tid] = c;
+                sn[tid] = s;
+            }
+            __syncthreads();
+            // rows p, q of A (the element walk of sym_eig_kernel)
+            for (int i = i0, j = j0; i < npairs;) {
+                const DFp s = sn[i];
+                if (s.hi != 0.f) {
+                    const DFp c = cs[i], ms = DFp{-s.hi, -s.lo};
+                    const int p = pp[i], q = qq[i];
+                    const DFp ap = A[p * k + j], aq = A[q * k + j];
+                    A[p * k + j] = dfp_dot2(c, ap, ms, aq);
+                    A[q * k + j] = dfp_dot2(s, ap, c, aq);
+                }
+                i += di;
+                j += dj;
+                if (j >= k) j -= k, ++i;
+            }
+            __syncthreads();
+            // columns p, q of A and V; the annihilated pair is set to zero exactly
+            for (int i = i0, j = j0; i < npairs;) {
+                const DFp s = sn[i];
+                if (s.hi != 0.f) {
+                    const DFp c = cs[i], ms = DFp{-s.hi, -s.lo};
+                    const int p = pp[i], q = qq[i];
+                    const DFp ap = A[j * k + p], aq = A[j * k + q];
+                    A[j * k + p] = j == q ? DFp{0.f, 0.f} : dfp_dot2(c, ap, ms, aq);
+                    A[j * k + q] = j == p ? DFp{0.f, 0.f} : dfp_dot2(s, ap, c, aq);
+                    const DFp vp = V[j * k + p], vq = V[j * k + q];
+                    V[j * k + p] = dfp_dot2(c, vp, ms, vq);
+                    V[j * k + q] = dfp_dot2(s, vp, c, vq);
+                }
+                i += di;
+                j += dj;
+                if (j >= k) j -= k, ++i;
+            }
+            __syncthreads();
+        }
+        if (!rotated) break;
+        __syncthreads();
+    }
+    if (tid == 0 && sweep >= kEigMaxSweeps) atomicCAS(err + 1, 0, 52);  // not converged
+    for (int i = tid; i < k; i += kEigThreads) dg[i] = dfp_val(A[i * k + i]) / sc;  // sc a power of two: exact
+    __syncthreads();
+    for (int i = tid; i < k; i += kEigThreads) {
+        int rank = 0;
+        for (int j = 0; j < k; ++j) rank += (dg[j] > dg[i] || (dg[j] == dg[i] && j < i)) ? 1 : 0;
+        ord[rank] = i;
+    }
+    __syncthreads();
+    for (int c = tid; c < k; c += kEigThreads) wout[c] = dg[ord[c]];
+    for (int e = tid; e < kk2; e += kEigThreads) {
+        const int i = e / k, c = e - i * k;
+        Wout[e] = dfp_val(V[i * k + ord[c]]);
+    }
+}
+
+// The k x k eigensolve on `stream`: the double-float kernel up to kEigDfMaxK, the FP64 kernel (V
+// in global scratch above kEigSmemK) beyond.  Measured at k = 40: 0.58 vs 1.20 ms per solve; at
+// k = 20: 0.10 vs 0.24 ms.
+constexpr int kEigDfMaxK = 48;
+
+static dpca_status eig_launch(const double *B, int k, double *W, double *w, double *vscratch, int *flags,
+                              cudaStream_t stream) {
+    if (k <= kEigDfMaxK) {
+        DPCA_TRY(allow_max_smem((const void *)sym_eig_df_kernel));
+        sym_eig_df_kernel<<<1, kEigThreads, (size_t)2 * k * k * sizeof(DFp), stream>>>(B, k, W, w, flags);
+    } else {
+        DPCA_TRY(allow_max_smem((const void *)sym_eig_kernel));
+        sym_eig_kernel<<<1, kEigThreads, eig_smem_bytes(k), stream>>>(B, k, W, w, vscratch, flags);
+    }
+    DPCA_CUDA(cudaGetLastError());
+    return DPCA_OK;
+}
+
 dpca_status launch_eig_desc(Handle *h) {
     ScopedLaunch t(&h->clock, h->stream, "sym_eig");
     const int k = h->k;
     const SmallLayout L{k};
-    DPCA_TRY(allow_max_smem((const void *)sym_eig_kernel));
     // V lives in global memory (the reduction scratch, >= k^2 doubles, free at this step) when
     // A and V do not both fit in shared memory
-    sym_eig_kernel<<<1, kEigThreads, eig_smem_bytes(k), h->stream>>>(h->small + L.B(), k, h->small + L.W(),
-                                                                       h->small + L.w(), h->red, h->dflag);
-    DPCA_CUDA(cudaGetLastError());
-    return DPCA_OK;
+    return eig_launch(h->small + L.B(), k, h->small + L.W(), h->small + L.w(), h->red, h->dflag, h->stream);
 }
 
 // ------------------------------------------------------------------ Omega = Q W
@@ -370,6 +594,97 @@ __global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__
     }
 }
 
+// The same factor and inverse in double-float arithmetic (the pairs of the Jacobi solver above),
+// for k <= kEigDfMaxK: its time is the pivot's dependent square root and reciprocal and the
+// inverse's dependent sums, which on this GPU's narrow FP64 pipe are the slow part.  G is scaled
+// by an even power of two 4^-e (max diagonal in [1/4, 1), FP32's exponent range), so R scales by
+// 2^-e and R^-1 by 2^e, both exactly; the shift uses the pairs' unit roundoff 2^-47 in place of
+// FP64's 2^-53, as the shifted CholeskyQR analysis asks of the working precision.  R^-1 comes out
+// to ~k 2^-47 relative, and the last two (unshifted) steps of CholeskyQR3 leave Q orthonormal to
+// that order, ~1e-13.
+__global__ void __launch_bounds__(kCholThreads) chol_inv_df_kernel(const double *__restrict__ G, int k, int n,
+                                                                   int always_shift, double *__restrict__ Rinv) {
+    extern __shared__ DFp Sd[];  // k x k pairs
+    __shared__ DFp pinv[kEigDfMaxK], col[kEigDfMaxK];
+    __shared__ double shift, gsc, rsc;
+    __shared__ int broke;
+    const int tid = threadIdx.x, kk2 = k * k;
+    if (tid == 0) {
+        double tr = 0.0, mx = 0.0;
+        for (int i = 0; i < k; ++i) {
+            tr += G[i * k + i];
+            mx = fmax(mx, fabs(G[i * k + i]));
+        }
+        int x = 0;
+        if (mx > 0.0 && isfinite(mx)) frexp(mx, &x);
+        const int e = (x + 1) >> 1;  // ceil(x / 2): mx 4^-e in [1/4, 1)
+        gsc = ldexp(1.0, -2 * e);
+        rsc = ldexp(1.0, -e);
+        shift = 11.0 * ((double)n * k + (double)k * (k + 1)) * 0x1p-47 * tr * gsc;
+    }
+    for (int attempt = always_shift ? 1 : 0; attempt < 2; ++attempt) {
+        __syncthreads();
+        for (int e = tid; e < kk2; e += kCholThreads) {
+            const int i = e / k, j = e - i * k;
+            Sd[e] = dfp_of(G[e] * gsc + (attempt == 1 && i == j ? shift : 0.0));
+        }
+        if (tid == 0) broke = 0;
+        __syncthreads();
+        for (int j = 0; j < k; ++j) {
+            if (tid == 0) {
+                DFp d = Sd[j * k + j];
+                if (!(d.hi > 0.f) || !isfinite(d.hi)) {
+                    if (attempt == 0) broke = 1;
+                    d = DFp{1.f, 0.f};
+                }
+                const DFp r = dfp_sqrt(d);
+                Sd[j * k + j] = r;
+                pinv[j] = dfp_div(DFp{1.f, 0.f}, r);
+            }
+            __syncthreads();
+            if (broke) break;  // block-uniform: read after the barrier
+            const DFp inv = pinv[j];
+            for (int c = j + 1 + tid; c < k; c += kCholThreads) Sd[j * k + c] = dfp_mul(Sd[j * k + c], inv);
+            __syncthreads();
+            for (int a = j + 1 + (tid >> 5); a < k; a += kCholThreads / 32) {
+                const DFp sa = Sd[j * k + a];
+                const DFp msa = DFp{-sa.hi, -sa.lo};
+                for (int c = a + (tid & 31); c < k; c += 32) Sd[a * k + c] = dfp_add(Sd[a * k + c], dfp_mul(msa, Sd[j * k + c]));
+            }
+            __syncthreads();
+        }
+        if (!broke) break;
+    }
+    int tw = 1;
+    while (tw < 32 && tw * 2 * k <= kCholThreads) tw *= 2;
+    const int team = tid / tw, lane = tid % tw, teams = kCholThreads / tw;
+    for (int j = 0; j < k; ++j) {
+        for (int i0 = 0; i0 < j; i0 += teams) {
+            const int i = i0 + team;
+            DFp sum = {0.f, 0.f};
+            if (i < j)
+                for (int l = i + lane; l < j; l += tw) sum = dfp_add(sum, dfp_mul(Sd[i * k + l], Sd[l * k + j]));
+            for (int o = tw >> 1; o > 0; o >>= 1) {
+                const DFp other = {__shfl_down_sync(0xffffffffu, sum.hi, o, tw), __shfl_down_sync(0xffffffffu, sum.lo, o, tw)};
+                sum = dfp_add(sum, other);
+            }
+            if (i < j && lane == 0) {
+                const DFp v = dfp_mul(sum, pinv[j]);
+                col[i] = DFp{-v.hi, -v.lo};
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < j; i += kCholThreads) Sd[i * k + j] = col[i];
+        if (tid == 0) Sd[j * k + j] = pinv[j];
+        __syncthreads();
+    }
+    const double r = rsc;
+    for (int e = tid; e < kk2; e += kCholThreads) {
+        const int i = e / k, j = e - i * k;
+        Rinv[e] = j >= i ? dfp_val(Sd[e]) * r : 0.0;
+    }
+}
+
 // ------------------------------------------------------------------ shifted CholeskyQR3
 // Thin QR of the n x k panel A (in place, Q only) by three CholeskyQR steps (Fukaya, Kannan,
 // Nakatsukasa, Yamamoto, Yanagisawa, "Shifted Cholesky QR for computing the QR factorization of
@@ -388,6 +703,7 @@ dpca_status launch_qr(Handle *h, double *a) {
     double *G = h->small + L.B(), *Rinv = h->small + L.W();  // free until the Rayleigh-Ritz step
     DPCA_TRY(allow_max_smem((const void *)apply_w_kernel));
     DPCA_TRY(allow_max_smem((const void *)chol_inv_kernel));
+    DPCA_TRY(allow_max_smem((const void *)chol_inv_df_kernel));
     const size_t smem_g = (size_t)k * k * sizeof(double);
     const int64_t total = (int64_t)n * k;
     const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
@@ -396,7 +712,10 @@ dpca_status launch_qr(Handle *h, double *a) {
         DPCA_TRY(atb_timed(h, src, src, n, G, "qr_gram", "qr_gram_sum"));
         {
             ScopedLaunch t(&h->clock, h->stream, "qr_chol");
-            chol_inv_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
+            if (k <= kEigDfMaxK)
+                chol_inv_df_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
+            else
+                chol_inv_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
             DPCA_CUDA(cudaGetLastError());
         }
         {
@@ -506,7 +825,7 @@ extern "C" dpca_status dpca_sym_eig_device(int device, int k, const double *b, d
         set_error("dpca_sym_eig_device: device allocation failed");
         return DPCA_ERR_NOMEM;
     }
-    dpca_status st = allow_max_smem((const void *)sym_eig_kernel);
+    dpca_status st = DPCA_OK;
     int hflags[16] = {0};
     cudaError_t e = cudaSuccess;
     if (st == DPCA_OK) {
@@ -514,8 +833,12 @@ extern "C" dpca_status dpca_sym_eig_device(int device, int k, const double *b, d
         e = cudaMemcpy(d, b, kk * sizeof(double), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemset(flags, 0, 16 * sizeof(int));
         if (e == cudaSuccess) {
-            sym_eig_kernel<<<1, kEigThreads, eig_smem_bytes(k)>>>(d, k, d + kk, d + 3 * kk, d + 2 * kk, flags);
-            e = cudaGetLastError();
+            st = eig_launch(d, k, d + kk, d + 3 * kk, d + 2 * kk, flags, 0);
+            if (st != DPCA_OK) {
+                cudaFree(d);
+                cudaFree(flags);
+                return st;
+            }
         }
         if (e == cudaSuccess) e = cudaMemcpy(W, d + kk, kk * sizeof(double), cudaMemcpyDeviceToHost);
         if (e == cudaSuccess) e = cudaMemcpy(w, d + 3 * kk, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost);

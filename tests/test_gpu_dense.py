@@ -1,7 +1,8 @@
 """The device k x k eigensolver of the Rayleigh-Ritz step (dpca_sym_eig_device) against LAPACK.
 
 Every outer iteration of a solve diagonalizes the k x k matrix B = Q^T Z on the device (parallel
-cyclic Jacobi in FP64, methods.cpp:981-1000 in the reference).  The cases are those of the host
+cyclic Jacobi, methods.cpp:981-1000 in the reference): in double-float arithmetic up to k = 48,
+in FP64 above (k = 48 and 49 are the boundary).  The cases are those of the host
 eigensolver's test: indefinite, positive semi-definite (like B), clustered and repeated
 eigenvalues, already diagonal, zero, and a nearly diagonal matrix (B from the second iteration
 on).  Tolerances as there: eigenvalues within 1e-12 of the largest, eigenvectors orthonormal and
@@ -30,7 +31,7 @@ def cases(k, rng):
     return out
 
 
-@pytest.mark.parametrize("k", [1, 2, 3, 8, 20, 40, 41, 97, 112, 113, 128])
+@pytest.mark.parametrize("k", [1, 2, 3, 8, 20, 40, 41, 47, 48, 49, 97, 112, 113, 128])
 def test_device_eig_matches_lapack(dpca, k):
     rng = np.random.default_rng(100 + k)
     for a in cases(k, rng):
