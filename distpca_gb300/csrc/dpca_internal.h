@@ -204,6 +204,9 @@ struct Handle {
     size_t dev_bytes = 0;
 
     KernelClock clock;
+    // Coarse timing of a solve's stages (a pass's two products, a QR, the eigensolve) when the
+    // per-launch clock is off: a few events per outer iteration instead of two per launch.
+    KernelClock *stage = nullptr;
 };
 
 // Raise a kernel's dynamic shared-memory limit to the current device's opt-in maximum, once

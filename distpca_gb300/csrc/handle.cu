@@ -484,14 +484,13 @@ dpca_status handle_pass_io(Handle *h, const double *in, double *out) {
         return DPCA_ERR_INVALID;
     }
     if (h->streamed) return streamed_pass(h, in, out);
-    if (h->precision == DPCA_PREC_FP64) {
-        DPCA_TRY(launch_fp64_xw(h, in, h->y));
-        DPCA_TRY(launch_fp64_xty(h, h->y, out));
-    } else {
-        DPCA_TRY(launch_mixed_xw(h, in, nullptr));
-        DPCA_TRY(launch_mixed_xty(h, out));
+    const bool fp64 = h->precision == DPCA_PREC_FP64;
+    {
+        ScopedLaunch t(h->stage, h->stream, fp64 ? "fp64_xw" : "mixed_xw");
+        DPCA_TRY(fp64 ? launch_fp64_xw(h, in, h->y) : launch_mixed_xw(h, in, nullptr));
     }
-    return DPCA_OK;
+    ScopedLaunch t(h->stage, h->stream, fp64 ? "fp64_xty" : "mixed_xty");
+    return fp64 ? launch_fp64_xty(h, h->y, out) : launch_mixed_xty(h, out);
 }
 
 dpca_status handle_pass(Handle *h) { return handle_pass_io(h, h->omega, h->z); }
@@ -544,9 +543,31 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     const bool in_core = cfg->bsize >= h->n_snp && !h->streamed;
     const size_t nkb = (size_t)n * k * sizeof(double);
     SmallLayout L{k};
+    // Statistics (the reference's timing block) come from the per-launch clock when the caller
+    // turned it on (profiling) or the handle streams (long passes), and otherwise from coarse
+    // stage events: two events around each of ~80 launches per outer iteration, and resolving
+    // them, cost the short solves of small cohorts ~15% of their time.
+    const bool fine = h->clock.enabled || h->streamed;
     bool clock_was = h->clock.enabled;
+    KernelClock coarse;
+    coarse.enabled = !fine;
+    h->stage = fine ? nullptr : &coarse;
+    // on every way out (errors included): no stage clock left pointing at this frame, and the
+    // caller's per-launch clock setting back
+    struct Restore {
+        Handle *h;
+        bool clock_was;
+        ~Restore() {
+            h->stage = nullptr;
+            h->clock.enabled = clock_was;
+        }
+    } restore{h, clock_was};
     h->clock.reset();
-    h->clock.enabled = true;
+    h->clock.enabled = fine;
+    auto qr = [&](double *a) {
+        ScopedLaunch t(h->stage, h->stream, "qr_chol");
+        return launch_qr(h, a);
+    };
     cudaEvent_t t0, t1;
     DPCA_CUDA(cudaEventCreate(&t0));
     DPCA_CUDA(cudaEventCreate(&t1));
@@ -558,7 +579,7 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     // later subspace and Ritz value -- is unchanged in exact arithmetic, but the reference's
     // start block is nearly rank-deficient (neighbouring columns come from neighbouring LCG
     // seeds), and a 22-bit product of it would lose its trailing directions.
-    if (h->precision == DPCA_PREC_MIXED) DPCA_TRY(launch_qr(h, h->omega));
+    if (h->precision == DPCA_PREC_MIXED) DPCA_TRY(qr(h->omega));
     double *omega = h->omega, *z = h->z, *q = h->q;
     int ii = 0, passes = 0;
     bool stopped = false;
@@ -566,23 +587,34 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
         DPCA_TRY(handle_pass_io(h, omega, z));
         passes++;
         for (int kk = 0; kk < power - 1; ++kk) {
-            DPCA_TRY(launch_qr(h, z));
+            DPCA_TRY(qr(z));
             std::swap(omega, z);  // Omega <- Q
             DPCA_TRY(handle_pass_io(h, omega, z));
             passes++;
         }
-        DPCA_TRY(launch_qr(h, z));
+        DPCA_TRY(qr(z));
         std::swap(q, z);  // Q
         if (in_core) {
-            DPCA_TRY(half_pass(h, q));
+            {
+                ScopedLaunch t(h->stage, h->stream, h->precision == DPCA_PREC_FP64 ? "fp64_xw" : "mixed_xw");
+                DPCA_TRY(half_pass(h, q));
+            }
+            ScopedLaunch t(h->stage, h->stream, "atb");
             DPCA_TRY(launch_atb(h, h->y, h->y, h->n_snp, h->small + L.B()));
         } else {
             DPCA_TRY(handle_pass_io(h, q, z));
             passes++;
+            ScopedLaunch t(h->stage, h->stream, "atb");
             DPCA_TRY(launch_atb(h, q, z, n, h->small + L.B()));
         }
-        DPCA_TRY(launch_eig_desc(h));
-        DPCA_TRY(launch_apply_w(h, q, omega));
+        {
+            ScopedLaunch t(h->stage, h->stream, "sym_eig");
+            DPCA_TRY(launch_eig_desc(h));
+        }
+        {
+            ScopedLaunch t(h->stage, h->stream, "apply_w");
+            DPCA_TRY(launch_apply_w(h, q, omega));
+        }
         DPCA_TRY(launch_sigma_and_criterion(h, nsv, crit, cfg->tol, ii, h->old, omega));
         DPCA_CUDA(cudaMemcpyAsync(h->host_small, h->small, L.total() * sizeof(double), cudaMemcpyDeviceToHost,
                                   h->stream));
@@ -625,7 +657,9 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
         for (int i = 0; i < n; ++i)
             for (int j = 0; j < nsv; ++j) res->u[(size_t)i * nsv + j] = omega_inout[(size_t)i * k + j];
     h->clock.resolve();
-    const KernelClock &c = h->clock;
+    coarse.resolve();
+    h->stage = nullptr;
+    const KernelClock &c = fine ? h->clock : coarse;
     double xw = slot_ms(c, "fp64_xw") + slot_ms(c, "mixed_xw") + slot_ms(c, "split_omega");
     double xty = slot_ms(c, "fp64_xty") + slot_ms(c, "reduce_splits") + slot_ms(c, "mixed_xty") +
                  slot_ms(c, "mixed_reduce");
