@@ -667,7 +667,7 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     res->time_mm_a_t = xty * 1e-3;
     res->time_mm = (xw + xty + slot_ms(c, "atb") + slot_ms(c, "atb_sum") + slot_ms(c, "apply_w")) * 1e-3;
     res->time_gs = (slot_ms(c, "qr_gram") + slot_ms(c, "qr_gram_sum") + slot_ms(c, "qr_chol") +
-                    slot_ms(c, "qr_apply")) * 1e-3;
+                    slot_ms(c, "qr_apply") + slot_ms(c, "qr_fused")) * 1e-3;
     res->time_projected_svd = slot_ms(c, "sym_eig") * 1e-3;
     res->time_other = total_ms * 1e-3 - res->time_mm - res->time_gs - res->time_projected_svd;
     if (res->time_other < 0) res->time_other = 0;

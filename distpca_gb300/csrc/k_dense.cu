@@ -14,18 +14,23 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "dpca_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace dpca {
 
 // ------------------------------------------------------------------ C = A^T B (k x k)
-// Block b accumulates rows [b*rpb, ...) into red[b][k*k]; outputs are spread over threads.
-__global__ void __launch_bounds__(256) atb_kernel(const double *__restrict__ A, const double *__restrict__ B, int n,
-                                                  int k, int rpb, double *__restrict__ part) {
-    extern __shared__ double tile[];  // [2][32][k]
+// Block b accumulates rows [b*rpb, ...) into red[b][k*k]; outputs are spread over threads.  The
+// block-level body is shared with the fused QR kernel below; `tile` is [2][32][k] doubles of shared
+// memory.
+__device__ __forceinline__ void atb_block(const double *__restrict__ A, const double *__restrict__ B, int n, int k,
+                                          int rpb, double *__restrict__ part, int bid, double *tile) {
     double *ta = tile, *tb = tile + 32 * k;
-    const int r0 = blockIdx.x * rpb, r1 = min(n, r0 + rpb);
+    const int r0 = bid * rpb, r1 = min(n, r0 + rpb);
     const int kk = k * k;
     for (int o0 = 0; o0 < kk; o0 += 256 * 8) {
         double acc[8];
@@ -54,17 +59,23 @@ __global__ void __launch_bounds__(256) atb_kernel(const double *__restrict__ A, 
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
             int o = o0 + threadIdx.x + 256 * m;
-            if (o < kk) part[(size_t)blockIdx.x * kk + o] = acc[m];
+            if (o < kk) part[(size_t)bid * kk + o] = acc[m];
         }
     }
+}
+
+__global__ void __launch_bounds__(256) atb_kernel(const double *__restrict__ A, const double *__restrict__ B, int n,
+                                                  int k, int rpb, double *__restrict__ part) {
+    extern __shared__ double tile[];  // [2][32][k]
+    atb_block(A, B, n, k, rpb, part, blockIdx.x, tile);
 }
 
 // out[e] = sum over p of part[p][e]: one warp per element, its lanes taking every 32nd part, then
 // a fixed-order shuffle reduction (deterministic).  With one thread per element the k^2 sums ran
 // on k^2 / 256 blocks, each thread walking all parts: ~36 us per Gram at 12,919 x 40, more than
 // the Gram itself.
-__global__ void __launch_bounds__(256) sum_parts_kernel(const double *__restrict__ part, int nparts, int elems,
-                                                        double *__restrict__ out) {
+__device__ __forceinline__ void sum_parts_body(const double *__restrict__ part, int nparts, int elems,
+                                               double *__restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < elems; e += warps) {
@@ -76,6 +87,22 @@ __global__ void __launch_bounds__(256) sum_parts_kernel(const double *__restrict
     }
 }
 
+__global__ void __launch_bounds__(256) sum_parts_kernel(const double *__restrict__ part, int nparts, int elems,
+                                                        double *__restrict__ out) {
+    sum_parts_body(part, nparts, elems, out);
+}
+
+// Row blocks of a Gram over n rows: as many as there are 32-row tiles, up to two per SM (FP64 is
+// a small fraction of this GPU's arithmetic: the n k^2 FMAs want many SMs), within the partials
+// buffer.
+static void gram_split(const Handle *h, int n, int *nparts, int *rpb) {
+    const int kk = h->k * h->k;
+    int np = std::max(1, std::min(2 * h->sm_count, ceil_div(n, 32)));
+    np = (int)std::min<int64_t>(np, (int64_t)(h->red_elems / kk));
+    *rpb = ceil_div(n, np);
+    *nparts = ceil_div(n, *rpb);
+}
+
 // A^T B over n rows in two launches (block partials, then their sum), timed under the given names.
 static dpca_status atb_timed(Handle *h, const double *a, const double *b, int n, double *out, const char *name,
                              const char *sum_name) {
@@ -83,10 +110,8 @@ static dpca_status atb_timed(Handle *h, const double *a, const double *b, int n,
     int kk = k * k;
     // FP64 is a small fraction of this GPU's arithmetic: spread the n k^2 FMAs over as many SMs
     // as there are 32-row tiles (up to two blocks per SM)
-    int nparts = std::max(1, std::min(2 * h->sm_count, ceil_div(n, 32)));
-    nparts = (int)std::min<int64_t>(nparts, (int64_t)(h->red_elems / kk));
-    int rpb = ceil_div(n, nparts);
-    nparts = ceil_div(n, rpb);
+    int nparts = 0, rpb = 0;
+    gram_split(h, n, &nparts, &rpb);
     size_t smem = (size_t)2 * 32 * k * sizeof(double);
     DPCA_TRY(allow_max_smem((const void *)atb_kernel));
     {
@@ -485,9 +510,8 @@ dpca_status launch_eig_desc(Handle *h) {
 }
 
 // ------------------------------------------------------------------ Omega = Q W
-__global__ void __launch_bounds__(256) apply_w_kernel(const double *__restrict__ Q, const double *__restrict__ W, int n,
-                                                      int k, double *__restrict__ out) {
-    extern __shared__ double ws[];
+__device__ __forceinline__ void apply_w_body(const double *__restrict__ Q, const double *__restrict__ W, int n, int k,
+                                             double *__restrict__ out, double *ws) {
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) ws[e] = W[e];
     __syncthreads();
     int64_t total = (int64_t)n * k;
@@ -499,6 +523,12 @@ __global__ void __launch_bounds__(256) apply_w_kernel(const double *__restrict__
         for (int a = 0; a < k; ++a) s = fma(q[a], ws[a * k + c], s);
         out[o] = s;
     }
+}
+
+__global__ void __launch_bounds__(256) apply_w_kernel(const double *__restrict__ Q, const double *__restrict__ W, int n,
+                                                      int k, double *__restrict__ out) {
+    extern __shared__ double ws[];
+    apply_w_body(Q, W, n, k, out, ws);
 }
 
 dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
@@ -524,9 +554,8 @@ dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
 // sum_{l=i..j-1} R^-1[i][l] R[l][j], each row's sum split over a team of lanes.
 constexpr int kCholThreads = 256;
 
-__global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__restrict__ G, int k, int n,
-                                                                int always_shift, double *__restrict__ Rinv) {
-    extern __shared__ double S[];  // k x k
+__device__ __forceinline__ void chol_inv_block(const double *__restrict__ G, int k, int n, int always_shift,
+                                               double *__restrict__ Rinv, double *S /* k x k shared */) {
     __shared__ double pinv[128], col[128];
     __shared__ double shift;
     __shared__ int broke;
@@ -602,9 +631,8 @@ __global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__
 // FP64's 2^-53, as the shifted CholeskyQR analysis asks of the working precision.  R^-1 comes out
 // to ~k 2^-47 relative, and the last two (unshifted) steps of CholeskyQR3 leave Q orthonormal to
 // that order, ~1e-13.
-__global__ void __launch_bounds__(kCholThreads) chol_inv_df_kernel(const double *__restrict__ G, int k, int n,
-                                                                   int always_shift, double *__restrict__ Rinv) {
-    extern __shared__ DFp Sd[];  // k x k pairs
+__device__ __forceinline__ void chol_inv_df_block(const double *__restrict__ G, int k, int n, int always_shift,
+                                                  double *__restrict__ Rinv, DFp *Sd /* k x k shared */) {
     __shared__ DFp pinv[kEigDfMaxK], col[kEigDfMaxK];
     __shared__ double shift, gsc, rsc;
     __shared__ int broke;
@@ -685,6 +713,52 @@ __global__ void __launch_bounds__(kCholThreads) chol_inv_df_kernel(const double 
     }
 }
 
+__global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__restrict__ G, int k, int n,
+                                                                int always_shift, double *__restrict__ Rinv) {
+    extern __shared__ double cS[];  // k x k
+    chol_inv_block(G, k, n, always_shift, Rinv, cS);
+}
+
+__global__ void __launch_bounds__(kCholThreads) chol_inv_df_kernel(const double *__restrict__ G, int k, int n,
+                                                                   int always_shift, double *__restrict__ Rinv) {
+    extern __shared__ DFp cSd[];  // k x k pairs
+    chol_inv_df_block(G, k, n, always_shift, Rinv, cSd);
+}
+
+// The whole shifted CholeskyQR3 of the panel `a` (n x k) in one cooperative launch: per step the
+// row-block Gram partials, their sum, the k x k factor and inverse (block 0; the other blocks wait
+// at the grid barrier), and A <- A R^-1, with a grid-wide barrier between stages; after the third
+// step the result is copied back into `a`.  The same stage bodies as the separate kernels, on the
+// same row blocks, so the result is bit-identical to them; it replaces 12 launches (and the copy)
+// per QR, whose launch gaps were most of a small panel's QR time.
+__global__ void __launch_bounds__(256) qr_fused_kernel(double *__restrict__ a, double *__restrict__ work, int n, int k,
+                                                       int nparts, int rpb, double *__restrict__ part,
+                                                       double *__restrict__ G, double *__restrict__ Rinv, int df) {
+    extern __shared__ __align__(16) unsigned char qsm[];
+    cg::grid_group grid = cg::this_grid();
+    double *src = a, *dst = work;
+    for (int step = 0; step < 3; ++step) {
+        if ((int)blockIdx.x < nparts) atb_block(src, src, n, k, rpb, part, blockIdx.x, (double *)qsm);
+        grid.sync();
+        sum_parts_body(part, nparts, k * k, G);
+        grid.sync();
+        if (blockIdx.x == 0) {
+            if (df) chol_inv_df_block(G, k, n, step == 0 ? 1 : 0, Rinv, (DFp *)qsm);
+            else chol_inv_block(G, k, n, step == 0 ? 1 : 0, Rinv, (double *)qsm);
+        }
+        grid.sync();
+        apply_w_body(src, Rinv, n, k, dst, (double *)qsm);
+        grid.sync();
+        double *t = src;
+        src = dst;
+        dst = t;
+    }
+    // three steps: a -> work -> a -> work
+    const int64_t total = (int64_t)n * k;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+        a[e] = src[e];
+}
+
 // ------------------------------------------------------------------ shifted CholeskyQR3
 // Thin QR of the n x k panel A (in place, Q only) by three CholeskyQR steps (Fukaya, Kannan,
 // Nakatsukasa, Yamamoto, Yanagisawa, "Shifted Cholesky QR for computing the QR factorization of
@@ -701,18 +775,44 @@ dpca_status launch_qr(Handle *h, double *a) {
     const int n = h->n_ind, k = h->k;
     const SmallLayout L{k};
     double *G = h->small + L.B(), *Rinv = h->small + L.W();  // free until the Rayleigh-Ritz step
+    const bool df = k <= kEigDfMaxK;
+    int nparts = 0, rpb = 0;
+    gram_split(h, n, &nparts, &rpb);
+    const size_t smem = std::max<size_t>((size_t)2 * 32 * k * sizeof(double), (size_t)k * k * sizeof(double));
+    // one cooperative launch while the grid (the Gram's row blocks, at least one block per SM for
+    // the apply) fits on the device at once; the separate kernels otherwise
+    if (h->qr_coresident == 0) {
+        int per_sm = 0;
+        DPCA_TRY(allow_max_smem((const void *)qr_fused_kernel));
+        DPCA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_fused_kernel, 256, smem));
+        h->qr_coresident = std::max(1, per_sm) * h->sm_count;
+        int coop = 0;
+        DPCA_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
+        if (!coop || per_sm < 1) h->qr_coresident = -1;
+    }
+    const int grid = std::max(nparts, h->sm_count);
+    if (h->qr_coresident > 0 && grid <= h->qr_coresident) {
+        ScopedLaunch t(&h->clock, h->stream, "qr_fused");
+        double *work = h->work;
+        int ni = n, ki = k, npi = nparts, rpbi = rpb, dfi = df ? 1 : 0;
+        double *red = h->red;
+        void *args[] = {&a, &work, &ni, &ki, &npi, &rpbi, &red, &G, &Rinv, &dfi};
+        DPCA_CUDA(cudaLaunchCooperativeKernel((const void *)qr_fused_kernel, dim3(grid), dim3(256), args, smem,
+                                              h->stream));
+        return DPCA_OK;
+    }
     DPCA_TRY(allow_max_smem((const void *)apply_w_kernel));
     DPCA_TRY(allow_max_smem((const void *)chol_inv_kernel));
     DPCA_TRY(allow_max_smem((const void *)chol_inv_df_kernel));
     const size_t smem_g = (size_t)k * k * sizeof(double);
     const int64_t total = (int64_t)n * k;
-    const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
+    const int agrid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
     double *src = a, *dst = h->work;
     for (int step = 0; step < 3; ++step) {
         DPCA_TRY(atb_timed(h, src, src, n, G, "qr_gram", "qr_gram_sum"));
         {
             ScopedLaunch t(&h->clock, h->stream, "qr_chol");
-            if (k <= kEigDfMaxK)
+            if (df)
                 chol_inv_df_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
             else
                 chol_inv_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
@@ -720,7 +820,7 @@ dpca_status launch_qr(Handle *h, double *a) {
         }
         {
             ScopedLaunch t(&h->clock, h->stream, "qr_apply");
-            apply_w_kernel<<<grid, 256, smem_g, h->stream>>>(src, Rinv, n, k, dst);
+            apply_w_kernel<<<agrid, 256, smem_g, h->stream>>>(src, Rinv, n, k, dst);
             DPCA_CUDA(cudaGetLastError());
         }
         std::swap(src, dst);
