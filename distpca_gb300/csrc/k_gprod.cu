@@ -503,12 +503,12 @@ __global__ void __launch_bounds__(128) gprod_bop_split_kernel(const float *__res
                                                               const unsigned int *__restrict__ colmax,
                                                               double *__restrict__ scales, __half *__restrict__ bop,
                                                               int *__restrict__ aq, long long *__restrict__ rq) {
-    __shared__ float scf[kMaxMixedNrhs];
+    __shared__ Pow2Pair scf[kMaxMixedNrhs];
     __shared__ long long rqs[kMaxMixedNrhs];
     __shared__ int tile[128 * (kMaxMixedNrhs + 1)];
     for (int c = threadIdx.x; c < k; c += blockDim.x) {
         const double sc = pow2_scale_below((double)__uint_as_float(colmax[c]) * 1.001);
-        scf[c] = (float)sc;
+        scf[c] = pow2_pair(sc);
         rqs[c] = 0;
         if (blockIdx.x == 0) {
             scales[2 * k + c] = sc;
@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(128) gprod_bop_split_kernel(const float *__res
         for (int c = 0; c < kp; ++c) {
             int na = 0;
             if (c < k) {
-                const float y = valid ? yt[(int64_t)c * ld + src] * scf[c] : 0.f;
+                const float y = valid ? yt[(int64_t)c * ld + src] * scf[c].a * scf[c].b : 0.f;
                 const int nb = __float2int_rn(b * y);
                 na = __float2int_rn(a * y);
                 const int h = (nb + 2048) >> 12;

@@ -512,11 +512,11 @@ __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict_
                                                         const unsigned int *__restrict__ colmax,
                                                         double *__restrict__ scales, __half *__restrict__ bop,
                                                         long long *__restrict__ rq) {
-    __shared__ float scf[kMaxMixedNrhs];
+    __shared__ Pow2Pair scf[kMaxMixedNrhs];
     __shared__ long long rqs[kMaxMixedNrhs];
     for (int c = threadIdx.x; c < k; c += blockDim.x) {
         const double sc = pow2_scale_below((double)__uint_as_float(colmax[c]) * 1.001);
-        scf[c] = (float)sc;  // a power of two: exact
+        scf[c] = pow2_pair(sc);  // powers of two: exact
         rqs[c] = 0;
         if (blockIdx.x == 0) {
             scales[2 * k + c] = sc;
@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(256) bop_split_kernel(const float *__restrict_
         const float a = valid ? (float)coef[2 * (size_t)src + 1] : 0.f;
         const float bma = b - a;
         for (int c = 0; c < k; ++c) {
-            const float y = valid ? yt[(int64_t)c * ld + src] * scf[c] : 0.f;
+            const float y = valid ? yt[(int64_t)c * ld + src] * scf[c].a * scf[c].b : 0.f;
             const int n1 = __float2int_rn(a * y), n2 = __float2int_rn(bma * y);
             const int h1 = (n1 + 2048) >> 12, h2 = (n2 + 2048) >> 12;
             bop[(int64_t)c * ld + s] = __int2half_rn(h2);
@@ -645,7 +645,8 @@ __global__ void __launch_bounds__(256) win_bop_split_kernel(const float *__restr
         const float a = valid ? (float)coef[2 * (size_t)src + 1] : 0.f;
         const float bma = b - a;
         for (int c = 0; c < k; ++c) {
-            const float y = valid ? yt[(int64_t)c * ld + src] * (float)sw[2 * k + c] : 0.f;
+            const Pow2Pair sp = pow2_pair(sw[2 * k + c]);
+            const float y = valid ? yt[(int64_t)c * ld + src] * sp.a * sp.b : 0.f;
             const int n1 = __float2int_rn(a * y), n2 = __float2int_rn(bma * y);
             const int h1 = (n1 + 2048) >> 12, h2 = (n2 + 2048) >> 12;
             bop[(int64_t)c * ld + s] = __int2half_rn(h2);

@@ -202,13 +202,24 @@ __device__ __forceinline__ DF df_from_double(double x) {
 
 // A power of two held in FP64 as FP32, by integer arithmetic on its exponent; 0 when it is not an
 // FP32 normal number (an Omega column below ~1e-31 or above ~1e45), for which the caller falls back
-// to FP64.  (Y itself is FP32, so the mixed pass serves Omega columns of about 1e-30 to 1e37; the
-// solver's Omega is orthonormal.)
+// to FP64.  (Y itself is FP32, so the mixed pass serves Omega columns whose Y = X Omega stays in
+// FP32's normal range, about 1e-37 to 1e37 for unit-variance columns; the solver's Omega is
+// orthonormal.)
 __device__ __forceinline__ float pow2_to_float(double x) {
     const long long bits = __double_as_longlong(x);
     const int e = (int)((bits >> 52) & 0x7FF) - 1023;
     if (e < -126 || e > 127) return 0.f;
     return __int_as_float((int)(bits >> 32 & 0x80000000) | ((e + 127) << 23));
+}
+
+// A power-of-two scale held in FP64 as two FP32 factors, so that (y * a) * b = y * scale exactly
+// wherever that product is an FP32 number: scales above 2^126 (the X^T Y operand of a Y column
+// whose largest |value| is below ~2^-103) overflow FP32 as one factor.
+struct Pow2Pair {
+    float a, b;
+};
+__device__ __forceinline__ Pow2Pair pow2_pair(double sc) {
+    return sc > 0x1p126 ? Pow2Pair{0x1p126f, (float)(sc * 0x1p-126)} : Pow2Pair{(float)sc, 1.f};
 }
 
 // c * x for an exact integer x (|x| < 2^48: x = H 2^24 + L with H, L exact in FP32).

@@ -11,6 +11,10 @@
                                                 of whole converged solves: the 1,000 x 100,000
                                                 cohort (nsv 10, nrhs 20, power 4, tol 1e-6) and
                                                 two serving-size jobs, mixed and FP64
+    python -m distpca_gb300.profcase stream     the 512 jobs of the serving stream (serve_stream,
+                                                seed 0) solved one at a time, mixed: wall time,
+                                                then per-kernel device time summed over the jobs
+                                                and split by job size
 
 Each case holds well under 1 GB on the device and launches each kernel a handful of times, so that
 an ncu capture of one launch (`-k <kernel> -c 1`) ends by itself in a minute or two.
@@ -78,7 +82,64 @@ def breakdown() -> None:
                               "kernel_ms_total": round(tot, 2), "per_kernel_ms_launches": per}), flush=True)
 
 
-CASES = {"incore": incore, "windows": windows, "breakdown": breakdown}
+def _kernel_family(name: str) -> str:
+    if name in ("mixed_xw", "mixed_xty", "mixed_reduce", "split_omega", "split_bop"):
+        return "products"
+    if name.startswith("qr"):
+        return "qr"
+    if name in ("atb", "sym_eig", "apply_w"):
+        return "rayleigh_ritz"
+    if name in ("synth_fill", "snp_stats", "transpose_packed"):
+        return "setup"
+    return "other"
+
+
+def stream() -> None:
+    jobs = synth.serve_stream(512, 50.0, seed=0)
+    cohorts = [synth.serve_cohort(j) for j in jobs]
+
+    def one(j, c, clock):
+        t0 = time.perf_counter()
+        with D.Handle(j["n_ind"], j["n_snp"], j["nrhs"], precision="mixed") as h:
+            if clock:
+                h.reset_kernel_times(True)
+            h.synth_fill(c)
+            r = h.solve(D.start_block(j["n_ind"], j["nrhs"]), nsv=j["nsv"], power=j["power"], bsize=j["n_snp"])
+            kt = h.kernel_times() if clock else {}
+        return time.perf_counter() - t0, r, kt
+
+    one(jobs[0], cohorts[0], False)  # warm-up: the library's one-time device setup
+    walls = np.array([one(j, c, False)[0] for j, c in zip(jobs, cohorts)])
+    print(json.dumps({"jobs": len(jobs), "one_at_a_time_s": round(float(walls.sum()), 3),
+                      "jobs_per_s": round(len(jobs) / float(walls.sum()), 2)}), flush=True)
+    geno = np.array([j["n_ind"] * j["n_snp"] for j in jobs], dtype=np.float64)
+    edges = np.quantile(geno, [0.25, 0.5, 0.75])
+    per_kernel: dict = {}
+    fam = np.zeros((4, 5))  # size quartile x (products, qr, rayleigh_ritz, setup, other)
+    names = ["products", "qr", "rayleigh_ritz", "setup", "other"]
+    passes = 0
+    for i, (j, c) in enumerate(zip(jobs, cohorts)):
+        _, r, kt = one(j, c, True)
+        passes += int(r["passes"])
+        q = int(np.searchsorted(edges, geno[i], side="right"))
+        for a, v in kt.items():
+            e = per_kernel.setdefault(a, [0.0, 0])
+            e[0] += v["ms"]
+            e[1] += v["launches"]
+            fam[q, names.index(_kernel_family(a))] += v["ms"]
+    tot = sum(v[0] for v in per_kernel.values())
+    print(json.dumps({"kernel_ms_total": round(tot, 1), "passes": passes,
+                      "per_kernel_ms_launches": {a: [round(v[0], 1), v[1]] for a, v in
+                                                 sorted(per_kernel.items(), key=lambda x: -x[1][0])}}), flush=True)
+    for q in range(4):
+        sel = np.searchsorted(edges, geno, side="right") == q
+        print(json.dumps({"size_quartile": q, "jobs": int(sel.sum()),
+                          "genotypes": [float(geno[sel].min()), float(geno[sel].max())],
+                          "one_at_a_time_s": round(float(walls[sel].sum()), 3),
+                          "kernel_ms": {n: round(float(fam[q, f]), 1) for f, n in enumerate(names)}}), flush=True)
+
+
+CASES = {"incore": incore, "windows": windows, "breakdown": breakdown, "stream": stream}
 
 
 def main(argv=None) -> int:

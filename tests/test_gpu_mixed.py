@@ -61,14 +61,15 @@ def test_pass_ragged_shapes_vs_fp64(dpca, n_ind, n_snp, k):
 
 def test_pass_columns_of_far_apart_magnitudes(dpca):
     """Each Omega column gets its own power-of-two fixed-point scale, and the X Omega epilogue
-    removes it by exponent arithmetic: columns from 1e-20 to 1e20 must each match the FP64 pass
-    to the per-column tolerance."""
+    removes it by exponent arithmetic: columns from 1e-33 to 1e20 must each match the FP64 pass
+    to the per-column tolerance.  At 1e-33 the scale's inverse (~2^-133) is below FP32's normal
+    range, so that column takes the epilogue's FP64 branch."""
     from distpca_gb300 import synth
 
-    n_ind, n_snp, k = 700, 3000, 6
+    n_ind, n_snp, k = 700, 3000, 7
     c = synth.make_cohort(n_ind, n_snp, n_pop=3, fst=0.05, missing=0.02, seed=11)
     packed = synth.pack_rows(c)
-    om = np.random.default_rng(3).standard_normal((n_ind, k)) * np.array([1e-20, 1e-9, 1.0, 3e5, 1e12, 1e20])
+    om = np.random.default_rng(3).standard_normal((n_ind, k)) * np.array([1e-33, 1e-20, 1e-9, 1.0, 3e5, 1e12, 1e20])
     with dpca.Handle(n_ind, n_snp, k, precision="fp64") as h:
         h.upload(packed)
         h.set_omega(om)
