@@ -17,7 +17,7 @@ import numpy as np
 
 __all__ = ["DpcaError", "Config", "Result", "Handle", "lib", "library_path", "config", "parse_args", "probe",
            "resolve", "start_block", "run", "run_packed", "decode_counts", "PREC_FP64", "PREC_MIXED",
-           "exported_symbols", "FullSVD", "full_svd", "Server", "JobInfo", "sym_eig", "Windows"]
+           "exported_symbols", "FullSVD", "full_svd", "Server", "JobInfo", "sym_eig", "qr_device", "Windows"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PREC_FP64 = 0
@@ -97,6 +97,7 @@ _SIGS = {
     "dpca_sym_eig": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "dpca_sym_eig_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p]),
+    "dpca_qr_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "dpca_run": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(Result)]),
     "dpca_run_packed": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(Result)]),
@@ -243,6 +244,15 @@ def sym_eig(b: np.ndarray, device: Optional[int] = None):
     else:
         _check(lib().dpca_sym_eig_device(device, k, _p(b), _p(w), _p(W)))
     return w, W
+
+
+def qr_device(a: np.ndarray, device: int = 0, separate: bool = False) -> np.ndarray:
+    """Q of the thin QR of the n x k panel a with the device kernels every solve uses (shifted
+    CholeskyQR3); `separate` runs it as separate kernels instead of one cooperative launch."""
+    q = np.array(a, dtype=np.float64, order="C", copy=True)
+    n, k = q.shape
+    _check(lib().dpca_qr_device(device, n, k, _p(q), 1 if separate else 0))
+    return q
 
 
 def _result_arrays(c: Config, n_ind: int):

@@ -827,6 +827,30 @@ dpca_status dpca_create_streamed(dpca_handle **out, int n_ind, int n_snp, int nr
     return DPCA_OK;
 }
 
+dpca_status dpca_qr_device(int device, int n, int k, double *a, int separate) {
+    clear_error();
+    if (n < 1 || k < 1 || k > kMaxNrhs || !a) {
+        set_error("dpca_qr_device: need n >= 1, 1 <= k <= %d and a non-null array", kMaxNrhs);
+        return DPCA_ERR_INVALID;
+    }
+    dpca_handle *hh = nullptr;
+    DPCA_TRY(dpca_create(&hh, n, 1, k, DPCA_PREC_FP64, device, nullptr));
+    Handle *h = &hh->h;
+    if (separate) h->qr_coresident = -1;
+    const size_t bytes = (size_t)n * k * sizeof(double);
+    dpca_status st = DPCA_OK;
+    cudaError_t e = cudaMemcpyAsync(h->omega, a, bytes, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) st = launch_qr(h, h->omega);
+    if (e == cudaSuccess && st == DPCA_OK) e = cudaMemcpyAsync(a, h->omega, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && st == DPCA_OK) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess && st == DPCA_OK) {
+        set_error("dpca_qr_device: %s", cudaGetErrorString(e));
+        st = DPCA_ERR_CUDA;
+    }
+    dpca_destroy(hh);
+    return st;
+}
+
 dpca_status dpca_destroy(dpca_handle *hh) {
     if (!hh) return DPCA_OK;
     cudaSetDevice(hh->h.device);

@@ -1,7 +1,8 @@
 // Small dense FP64 steps of the subspace iteration (methods.cpp:944-1063), all on the device:
-//   launch_qr         thin QR of the n x k panel by shifted CholeskyQR3: atb_kernel (Gram),
-//                     chol_inv_kernel (the k x k Cholesky factor and its inverse, one block) and
-//                     apply_w_kernel (A R^-1), three times (methods.cpp:947-961, see launch_qr).
+//   launch_qr         thin QR of the n x k panel by shifted CholeskyQR3: the Gram, the k x k
+//                     Cholesky factor and its inverse (one block) and A R^-1, three times, in one
+//                     cooperative launch (qr_fused_kernel) or as separate kernels
+//                     (methods.cpp:947-961, see launch_qr).
 //   atb_kernel        C = A^T B over the n rows (B = Q^T Z, methods.cpp:972-973; the in-core
 //                     Gram (XQ)^T (XQ), methods.cpp:141-142).
 //   launch_eig_desc   the k x k eigenproblem (dsyev 'V','U' and the column reversal,
@@ -24,33 +25,60 @@ namespace cg = cooperative_groups;
 namespace dpca {
 
 // ------------------------------------------------------------------ C = A^T B (k x k)
+// Upper-triangle entry t (row-major, diagonal included) of a k x k matrix: row a is the largest
+// with a (2k - a + 1) / 2 <= t, from a single-precision estimate corrected by whole steps.
+__device__ __forceinline__ void tri_index(int t, int k, int &a, int &c) {
+    const float b = 2.f * (float)k + 1.f;
+    int x = (int)((b - sqrtf(fmaxf(b * b - 8.f * (float)t, 0.f))) * 0.5f);
+    x = max(0, min(x, k - 1));
+    while (x > 0 && x * (2 * k - x + 1) / 2 > t) --x;
+    while (x + 1 < k && (x + 1) * (2 * k - x) / 2 <= t) ++x;
+    a = x;
+    c = t - x * (2 * k - x + 1) / 2 + x;
+}
+
 // Block b accumulates rows [b*rpb, ...) into red[b][k*k]; outputs are spread over threads.  The
 // block-level body is shared with the fused QR kernel below; `tile` is [2][32][k] doubles of shared
-// memory.
+// memory.  With `sym` (B == A, a Gram matrix) only the upper triangle's k (k + 1) / 2 sums are
+// formed and each is written to both mirrored places: x y == y x in floating point, so the result
+// has the bits of the full product at half the FMAs.
 __device__ __forceinline__ void atb_block(const double *__restrict__ A, const double *__restrict__ B, int n, int k,
-                                          int rpb, double *__restrict__ part, int bid, double *tile) {
-    double *ta = tile, *tb = tile + 32 * k;
+                                          int rpb, double *__restrict__ part, int bid, double *tile, bool sym) {
+    double *ta = tile, *tb = sym ? tile : tile + 32 * k;
     const int r0 = bid * rpb, r1 = min(n, r0 + rpb);
-    const int kk = k * k;
-    for (int o0 = 0; o0 < kk; o0 += 256 * 8) {
+    const int kk = k * k, outs = sym ? k * (k + 1) / 2 : kk;
+    for (int o0 = 0; o0 < outs; o0 += 256 * 8) {
         double acc[8];
+        int oa[8], oc[8];
 #pragma unroll
-        for (int m = 0; m < 8; ++m) acc[m] = 0.0;
+        for (int m = 0; m < 8; ++m) {
+            acc[m] = 0.0;
+            const int o = o0 + threadIdx.x + 256 * m;
+            oa[m] = oc[m] = 0;
+            if (o < outs) {
+                if (sym) {
+                    tri_index(o, k, oa[m], oc[m]);
+                } else {
+                    oa[m] = o / k;
+                    oc[m] = o - oa[m] * k;
+                }
+            }
+        }
         for (int i0 = r0; i0 < r1; i0 += 32) {
             __syncthreads();
             for (int e = threadIdx.x; e < 32 * k; e += 256) {
                 int ii = e / k, c = e - ii * k;
                 int i = i0 + ii;
                 ta[e] = i < r1 ? A[(size_t)i * k + c] : 0.0;
-                tb[e] = i < r1 ? B[(size_t)i * k + c] : 0.0;
+                if (!sym) tb[e] = i < r1 ? B[(size_t)i * k + c] : 0.0;
             }
             __syncthreads();
 #pragma unroll
             for (int m = 0; m < 8; ++m) {
-                int o = o0 + threadIdx.x + 256 * m;
-                if (o < kk) {
-                    int a = o / k, c = o - a * k;
+                if (o0 + (int)threadIdx.x + 256 * m < outs) {
+                    const int a = oa[m], c = oc[m];
                     double s = acc[m];
+#pragma unroll 1
                     for (int ii = 0; ii < 32; ++ii) s = fma(ta[ii * k + a], tb[ii * k + c], s);
                     acc[m] = s;
                 }
@@ -58,8 +86,10 @@ __device__ __forceinline__ void atb_block(const double *__restrict__ A, const do
         }
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
-            int o = o0 + threadIdx.x + 256 * m;
-            if (o < kk) part[(size_t)bid * kk + o] = acc[m];
+            if (o0 + (int)threadIdx.x + 256 * m < outs) {
+                part[(size_t)bid * kk + oa[m] * k + oc[m]] = acc[m];
+                if (sym && oa[m] != oc[m]) part[(size_t)bid * kk + oc[m] * k + oa[m]] = acc[m];
+            }
         }
     }
 }
@@ -67,7 +97,7 @@ __device__ __forceinline__ void atb_block(const double *__restrict__ A, const do
 __global__ void __launch_bounds__(256) atb_kernel(const double *__restrict__ A, const double *__restrict__ B, int n,
                                                   int k, int rpb, double *__restrict__ part) {
     extern __shared__ double tile[];  // [2][32][k]
-    atb_block(A, B, n, k, rpb, part, blockIdx.x, tile);
+    atb_block(A, B, n, k, rpb, part, blockIdx.x, tile, A == B);
 }
 
 // out[e] = sum over p of part[p][e]: one warp per element, its lanes taking every 32nd part, then
@@ -278,11 +308,11 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const double *__re
 // rate, and the row and column updates -- ~5 k^2 FMAs per round, all of the solve's arithmetic --
 // bound the FP64 kernel on its one SM together with the rotations' dependent FP64 division and
 // square-root chains (a warp's FP64 instruction occupies the narrow FP64 pipe for many cycles).
-// The rotations are formed in double-float too: an FP32 root or quotient and one compensated
-// correction each.  The relative skip test uses 2^-44 in place of FP64's epsilon, with an absolute
+// The rotations are formed in double-float too, from reciprocal square roots and quotients
+// refined by Newton steps in pairs (dfp_rsqrt, dfp_div_fast).  The relative skip test uses 2^-44 in place of FP64's epsilon, with an absolute
 // floor of 2^-47, so the sweeps end at the pairs' precision.  B is scaled by a power of two to
 // max |b| in [1/2, 1) first (FP32's exponent range), and the eigenvalues scaled back exactly.
-// Each rotation's c^2 + s^2 is 1 within ~2^-46, and that error compounds over the ~2k rotations an
+// Each rotation's c^2 + s^2 is 1 within ~2^-45, and that error compounds over the ~2k rotations an
 // entry takes per sweep: eigenvalues and eigenvectors come out within 1e-12 of max |w| up to k = 48
 // (checked against LAPACK in the tests, as the FP64 kernel), ~2e-12 at k = 97.  So this kernel
 // serves k <= kEigDfMaxK -- every mixed-precision width and the usual nrhs -- and the FP64 kernel
@@ -332,20 +362,40 @@ __device__ __forceinline__ DFp dfp_mul(DFp a, DFp b) {
     return dfp_fast_two_sum(p, e);
 }
 
-// a / b: an FP32 quotient and one correction from the exact-ish remainder a - q b
-__device__ __forceinline__ DFp dfp_div(DFp a, DFp b) {
-    const float q1 = __fdiv_rn(a.hi, b.hi);
-    const DFp r = dfp_add(a, dfp_mul(b, DFp{-q1, 0.f}));
-    return dfp_fast_two_sum(q1, __fdiv_rn(r.hi, b.hi));
+// The pivots and rotation angles below are dependent chains.  Built on the correctly rounded FP32
+// square root and quotient (multi-instruction sequences), they were the cost of the k x k kernels;
+// these forms start from the hardware's approximate reciprocal square root and reciprocal instead
+// and refine in pairs.
+
+// 1/sqrt(a) for a pair a > 0: rsqrtf's estimate, one Newton step x' = x + x (1 - a x^2) / 2 in
+// FP32, and one more with the residual 1 - a x^2 formed from the exact square of x in pairs
+// (Newton's iteration for x^-2 = a; the second step squares the first one's ~2^-23 error): within
+// ~2^-45.5 relative.  An a below 2^-100 (subnormal ones included) is scaled by 2^100 first and the
+// result by 2^50, so that x^2 stays inside FP32's range; both scalings are exact.
+__device__ __forceinline__ DFp dfp_rsqrt(DFp a) {
+    const bool tiny = a.hi < 0x1p-100f;
+    if (tiny) a = DFp{__fmul_rn(a.hi, 0x1p100f), __fmul_rn(a.lo, 0x1p100f)};
+    float x = rsqrtf(a.hi);
+    x = __fmaf_rn(__fmul_rn(0.5f, x), __fmaf_rn(-a.hi, __fmul_rn(x, x), 1.f), x);
+    const float p = __fmul_rn(x, x), pe = __fmaf_rn(x, x, -p);  // x^2 = p + pe exactly
+    const DFp q = dfp_mul(a, DFp{p, pe});                        // a x^2, within 2^-22 of 1
+    const float r = __fsub_rn(__fsub_rn(1.f, q.hi), q.lo);        // 1 - q.hi is exact (Sterbenz)
+    DFp y = dfp_fast_two_sum(x, __fmul_rn(__fmul_rn(0.5f, x), r));
+    if (tiny) y = DFp{__fmul_rn(y.hi, 0x1p50f), __fmul_rn(y.lo, 0x1p50f)};
+    return y;
 }
 
-// sqrt(a), a >= 0: the correctly rounded FP32 root x and one Newton correction (a - x^2) / 2x
-__device__ __forceinline__ DFp dfp_sqrt(DFp a) {
-    if (!(a.hi > 0.f)) return DFp{0.f, 0.f};
-    const float x = __fsqrt_rn(a.hi);
-    const float p = __fmul_rn(x, x), pe = __fmaf_rn(x, x, -p);
-    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), a.lo);
-    return dfp_fast_two_sum(x, __fdiv_rn(r, __fmul_rn(2.f, x)));
+// a / b for pairs, b != 0 and a / b inside FP32's normal range: q1 = a.hi times an approximate
+// reciprocal of b.hi, then two corrections q += (a - q b) / b from remainders formed in pairs,
+// each dividing by the same approximate reciprocal (each step multiplies the relative error by
+// ~2^-21): ~2^-46 relative.
+__device__ __forceinline__ DFp dfp_div_fast(DFp a, DFp b) {
+    const float rb = __fdividef(1.f, b.hi);
+    const float q1 = __fmul_rn(a.hi, rb);
+    const DFp r1 = dfp_add(a, dfp_mul(b, DFp{-q1, 0.f}));
+    const DFp q = dfp_fast_two_sum(q1, __fmul_rn(r1.hi, rb));
+    const DFp r2 = dfp_add(a, dfp_mul(b, DFp{-q.hi, -q.lo}));
+    return dfp_add(q, DFp{__fmul_rn(r2.hi, rb), 0.f});
 }
 
 __global__ void __launch_bounds__(kEigThreads) sym_eig_df_kernel(const double *__restrict__ Bin, int k,
@@ -415,10 +465,11 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_df_kernel(const double *_
                         const DFp ad = d.hi < 0.f ? DFp{-d.hi, -d.lo} : d;
                         const DFp aa = apq.hi < 0.f ? DFp{-apq.hi, -apq.lo} : apq;
                         const DFp two_a = {2.f * aa.hi, 2.f * aa.lo};
-                        const DFp rt = dfp_sqrt(dfp_add(dfp_mul(ad, ad), dfp_mul(two_a, two_a)));
-                        DFp t = dfp_div(two_a, dfp_add(ad, rt));
+                        const DFp h2 = dfp_add(dfp_mul(ad, ad), dfp_mul(two_a, two_a));
+                        const DFp rt = dfp_mul(h2, dfp_rsqrt(h2));  // sqrt(d^2 + 4 a_pq^2)
+                        DFp t = dfp_div_fast(two_a, dfp_add(ad, rt));
                         if (neg) t = DFp{-t.hi, -t.lo};
-                        c = dfp_div(DFp{1.f, 0.f}, dfp_sqrt(dfp_add(DFp{1.f, 0.f}, dfp_mul(t, t))));
+                        c = dfp_rsqrt(dfp_add(DFp{1.f, 0.f}, dfp_mul(t, t)));
                         s = dfp_mul(t, c);
                         if (s.hi != 0.f) rotated = 1;
                     }
@@ -510,25 +561,31 @@ dpca_status launch_eig_desc(Handle *h) {
 }
 
 // ------------------------------------------------------------------ Omega = Q W
+// With `upper` (W upper triangular, as R^-1 in the QR) the sum of column c stops at row c: the
+// terms past it are fma(q, 0, s) = s for finite q, so the bits are those of the full sum at about
+// half the FMAs.
 __device__ __forceinline__ void apply_w_body(const double *__restrict__ Q, const double *__restrict__ W, int n, int k,
-                                             double *__restrict__ out, double *ws) {
-    for (int e = threadIdx.x; e < k * k; e += blockDim.x) ws[e] = W[e];
-    __syncthreads();
+                                             double *__restrict__ out, double *ws, bool upper = false) {
+    if (W) {  // else ws already holds it
+        for (int e = threadIdx.x; e < k * k; e += blockDim.x) ws[e] = W[e];
+        __syncthreads();
+    }
     int64_t total = (int64_t)n * k;
     for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
         int64_t i = o / k;
         int c = (int)(o - i * k);
         const double *q = Q + i * k;
         double s = 0.0;
-        for (int a = 0; a < k; ++a) s = fma(q[a], ws[a * k + c], s);
+        const int end = upper ? c + 1 : k;
+        for (int a = 0; a < end; ++a) s = fma(q[a], ws[a * k + c], s);
         out[o] = s;
     }
 }
 
 __global__ void __launch_bounds__(256) apply_w_kernel(const double *__restrict__ Q, const double *__restrict__ W, int n,
-                                                      int k, double *__restrict__ out) {
+                                                      int k, double *__restrict__ out, int upper) {
     extern __shared__ double ws[];
-    apply_w_body(Q, W, n, k, out, ws);
+    apply_w_body(Q, W, n, k, out, ws, upper != 0);
 }
 
 dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
@@ -538,7 +595,7 @@ dpca_status launch_apply_w(Handle *h, const double *q, double *out) {
     DPCA_TRY(allow_max_smem((const void *)apply_w_kernel));
     int64_t total = (int64_t)h->n_ind * k;
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 4);
-    apply_w_kernel<<<grid, 256, smem, h->stream>>>(q, h->small + SmallLayout{k}.W(), h->n_ind, k, out);
+    apply_w_kernel<<<grid, 256, smem, h->stream>>>(q, h->small + SmallLayout{k}.W(), h->n_ind, k, out, 0);
     DPCA_CUDA(cudaGetLastError());
     return DPCA_OK;
 }
@@ -624,19 +681,38 @@ __device__ __forceinline__ void chol_inv_block(const double *__restrict__ G, int
 }
 
 // The same factor and inverse in double-float arithmetic (the pairs of the Jacobi solver above),
-// for k <= kEigDfMaxK: its time is the pivot's dependent square root and reciprocal and the
-// inverse's dependent sums, which on this GPU's narrow FP64 pipe are the slow part.  G is scaled
-// by an even power of two 4^-e (max diagonal in [1/4, 1), FP32's exponent range), so R scales by
-// 2^-e and R^-1 by 2^e, both exactly; the shift uses the pairs' unit roundoff 2^-47 in place of
-// FP64's 2^-53, as the shifted CholeskyQR analysis asks of the working precision.  R^-1 comes out
-// to ~k 2^-47 relative, and the last two (unshifted) steps of CholeskyQR3 leave Q orthonormal to
-// that order, ~1e-13.
+// for k <= kEigDfMaxK.  G is scaled by an even power of two 4^-e (max diagonal in [1/4, 1), FP32's
+// exponent range), so R scales by 2^-e and R^-1 by 2^e, both exactly; the shift uses the pairs'
+// unit roundoff 2^-47 in place of FP64's 2^-53, as the shifted CholeskyQR analysis asks of the
+// working precision.  R^-1 comes out to ~k 2^-47 relative, and the last two (unshifted) steps of
+// CholeskyQR3 leave Q orthonormal to that order, ~1e-13.
+//
+// One barrier per column: step j's pivot 1/r = 1/sqrt(d_j) (dfp_rsqrt) and r = d_j / r are taken
+// by every thread from the same d_j (the same operations, so the same bits in every thread), row j
+// of R is written to its own array while the trailing update recomputes the scaled entries it
+// needs, and column j of R^-1 (from R's column j and the inverse's columns before it, written by
+// earlier steps) is formed in the same step.  The arithmetic of every entry is that of a
+// factorization followed by a column-by-column inversion with the scaled row held in place: only
+// the waits are fewer.  The trailing update loads a warp's rows (at most kRowsPerWarp of them)
+// before storing any, so that their independent chains overlap.
+//
+// Rank deficiency.  The first (shifted) step has every pivot above the shift.  In the unshifted
+// steps a pivot at or below kPivotFloor (the scaled Gram's largest diagonal is in [1/4, 1), and
+// these steps' Grams are near the identity) means a column that is numerically a combination of
+// the columns before it -- an exactly rank-deficient panel, such as a full-width block whose
+// cohort has fewer independent directions than columns.  Its pivot is replaced by kPivotFloor:
+// that column comes out as rescaled rounding noise, which the next step orthonormalizes against
+// the others, while every other column keeps its exact normalisation.  (A sign change of that
+// noise-level pivot, from last-bit differences, used to send the whole step to a shifted retry,
+// which shrinks every column by ~shift / (2 diag): 4e-9 for a 37-column full-width panel.)
+constexpr int kRowsPerWarp = (kEigDfMaxK + kCholThreads / 32 - 1) / (kCholThreads / 32);
+constexpr float kPivotFloor = 0x1p-47f;
+
 __device__ __forceinline__ void chol_inv_df_block(const double *__restrict__ G, int k, int n, int always_shift,
-                                                  double *__restrict__ Rinv, DFp *Sd /* k x k shared */) {
-    __shared__ DFp pinv[kEigDfMaxK], col[kEigDfMaxK];
+                                                  double *__restrict__ Rinv, DFp *Sd /* 3 k x k shared */) {
     __shared__ double shift, gsc, rsc;
-    __shared__ int broke;
-    const int tid = threadIdx.x, kk2 = k * k;
+    DFp *Rd = Sd + k * k, *Xd = Rd + k * k;
+    const int tid = threadIdx.x, warp = tid >> 5, wl = tid & 31, kk2 = k * k;
     if (tid == 0) {
         double tr = 0.0, mx = 0.0;
         for (int i = 0; i < k; ++i) {
@@ -650,84 +726,131 @@ __device__ __forceinline__ void chol_inv_df_block(const double *__restrict__ G, 
         rsc = ldexp(1.0, -e);
         shift = 11.0 * ((double)n * k + (double)k * (k + 1)) * 0x1p-47 * tr * gsc;
     }
-    for (int attempt = always_shift ? 1 : 0; attempt < 2; ++attempt) {
-        __syncthreads();
-        for (int e = tid; e < kk2; e += kCholThreads) {
-            const int i = e / k, j = e - i * k;
-            Sd[e] = dfp_of(G[e] * gsc + (attempt == 1 && i == j ? shift : 0.0));
-        }
-        if (tid == 0) broke = 0;
-        __syncthreads();
-        for (int j = 0; j < k; ++j) {
-            if (tid == 0) {
-                DFp d = Sd[j * k + j];
-                if (!(d.hi > 0.f) || !isfinite(d.hi)) {
-                    if (attempt == 0) broke = 1;
-                    d = DFp{1.f, 0.f};
-                }
-                const DFp r = dfp_sqrt(d);
-                Sd[j * k + j] = r;
-                pinv[j] = dfp_div(DFp{1.f, 0.f}, r);
-            }
-            __syncthreads();
-            if (broke) break;  // block-uniform: read after the barrier
-            const DFp inv = pinv[j];
-            for (int c = j + 1 + tid; c < k; c += kCholThreads) Sd[j * k + c] = dfp_mul(Sd[j * k + c], inv);
-            __syncthreads();
-            for (int a = j + 1 + (tid >> 5); a < k; a += kCholThreads / 32) {
-                const DFp sa = Sd[j * k + a];
-                const DFp msa = DFp{-sa.hi, -sa.lo};
-                for (int c = a + (tid & 31); c < k; c += 32) Sd[a * k + c] = dfp_add(Sd[a * k + c], dfp_mul(msa, Sd[j * k + c]));
-            }
-            __syncthreads();
-        }
-        if (!broke) break;
-    }
+    // inverse: teams of `tw` lanes (a power of two <= 32) share a row's sum
     int tw = 1;
     while (tw < 32 && tw * 2 * k <= kCholThreads) tw *= 2;
     const int team = tid / tw, lane = tid % tw, teams = kCholThreads / tw;
-    for (int j = 0; j < k; ++j) {
-        for (int i0 = 0; i0 < j; i0 += teams) {
-            const int i = i0 + team;
-            DFp sum = {0.f, 0.f};
-            if (i < j)
-                for (int l = i + lane; l < j; l += tw) sum = dfp_add(sum, dfp_mul(Sd[i * k + l], Sd[l * k + j]));
-            for (int o = tw >> 1; o > 0; o >>= 1) {
-                const DFp other = {__shfl_down_sync(0xffffffffu, sum.hi, o, tw), __shfl_down_sync(0xffffffffu, sum.lo, o, tw)};
-                sum = dfp_add(sum, other);
-            }
-            if (i < j && lane == 0) {
-                const DFp v = dfp_mul(sum, pinv[j]);
-                col[i] = DFp{-v.hi, -v.lo};
-            }
+    {
+        __syncthreads();
+        for (int e = tid; e < kk2; e += kCholThreads) {
+            const int i = e / k, j = e - i * k;
+            Sd[e] = dfp_of(G[e] * gsc + (always_shift && i == j ? shift : 0.0));
         }
         __syncthreads();
-        for (int i = tid; i < j; i += kCholThreads) Sd[i * k + j] = col[i];
-        if (tid == 0) Sd[j * k + j] = pinv[j];
-        __syncthreads();
+        for (int j = 0; j < k; ++j) {
+            DFp d = Sd[j * k + j];  // the same value in every thread
+            if (!(d.hi > (always_shift ? 0.f : kPivotFloor)) || !isfinite(d.hi))
+                d = always_shift ? DFp{1.f, 0.f} : DFp{kPivotFloor, 0.f};
+            const DFp inv = dfp_rsqrt(d);  // 1 / R[j][j]
+            const DFp r = dfp_mul(d, inv);  // R[j][j]
+            for (int c = j + tid; c < k; c += kCholThreads) Rd[j * k + c] = c == j ? r : dfp_mul(Sd[j * k + c], inv);
+            // trailing upper triangle: a warp per row (rows j+1+warp, +8, ...), lanes over columns
+            {
+                DFp msa[kRowsPerWarp], sv[kRowsPerWarp][2];
+                const DFp r0 = wl + 0 < k ? dfp_mul(Sd[j * k + wl], inv) : DFp{0.f, 0.f};
+                const DFp r1 = wl + 32 < k ? dfp_mul(Sd[j * k + wl + 32], inv) : DFp{0.f, 0.f};
+#pragma unroll
+                for (int q = 0; q < kRowsPerWarp; ++q) {
+                    const int a = j + 1 + warp + q * (kCholThreads / 32);
+                    if (a < k) {
+                        const DFp sa = dfp_mul(Sd[j * k + a], inv);
+                        msa[q] = DFp{-sa.hi, -sa.lo};
+                        sv[q][0] = wl >= a && wl < k ? Sd[a * k + wl] : DFp{0.f, 0.f};
+                        sv[q][1] = wl + 32 >= a && wl + 32 < k ? Sd[a * k + wl + 32] : DFp{0.f, 0.f};
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < kRowsPerWarp; ++q) {
+                    const int a = j + 1 + warp + q * (kCholThreads / 32);
+                    if (a < k) {
+                        if (wl >= a && wl < k) Sd[a * k + wl] = dfp_add(sv[q][0], dfp_mul(msa[q], r0));
+                        if (wl + 32 >= a && wl + 32 < k) Sd[a * k + wl + 32] = dfp_add(sv[q][1], dfp_mul(msa[q], r1));
+                    }
+                }
+            }
+            // column j of R^-1: X[i][j] = -(sum over l in [i, j) of X[i][l] R[l][j]) / R[j][j]
+            for (int i0 = 0; i0 < j; i0 += teams) {
+                const int i = i0 + team;
+                DFp sum = {0.f, 0.f};
+                if (i < j)
+                    for (int l = i + lane; l < j; l += tw) sum = dfp_add(sum, dfp_mul(Xd[i * k + l], Rd[l * k + j]));
+                for (int o = tw >> 1; o > 0; o >>= 1) {
+                    const DFp other = {__shfl_down_sync(0xffffffffu, sum.hi, o, tw),
+                                       __shfl_down_sync(0xffffffffu, sum.lo, o, tw)};
+                    sum = dfp_add(sum, other);
+                }
+                if (i < j && lane == 0) {
+                    const DFp v = dfp_mul(sum, inv);
+                    Xd[i * k + j] = DFp{-v.hi, -v.lo};
+                }
+            }
+            if (tid == 0) Xd[j * k + j] = inv;
+            __syncthreads();
+        }
     }
     const double r = rsc;
     for (int e = tid; e < kk2; e += kCholThreads) {
         const int i = e / k, j = e - i * k;
-        Rinv[e] = j >= i ? dfp_val(Sd[e]) * r : 0.0;
+        Rinv[e] = j >= i ? dfp_val(Xd[e]) * r : 0.0;
+    }
+}
+
+// A Gram matrix of a panel whose columns are already orthonormal to within kNearIdentity (the
+// third CholeskyQR step, and often the second) skips the factorization: with G = I + E, R = I + F
+// for F the upper triangle of E with its diagonal halved has R^T R = I + E + F^T F, so R^-1 = I - F
+// to O(|E|^2) < k 2^-56, and Q = A (I - F) has Q^T Q = I + O(|E|^2).
+constexpr double kNearIdentity = 0x1p-28;
+
+// Largest |G - I| entry, block-wide: every thread gets it (a NaN counts as infinite).
+__device__ __forceinline__ double gram_defect(const double *__restrict__ G, int k) {
+    __shared__ double buf[32];
+    double m = 0.0;
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int i = e / k, c = e - i * k;
+        const double d = fabs(G[e] - (i == c ? 1.0 : 0.0));
+        m = d <= m ? m : (d == d ? d : INFINITY);
+    }
+    m = warp_max(m);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) buf[threadIdx.x >> 5] = m;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, buf[w]);
+    return t;
+}
+
+// R^-1 = I - F (upper triangular, row-major) for a G within kNearIdentity of the identity.
+__device__ __forceinline__ void rinv_near_identity(const double *__restrict__ G, int k, double *__restrict__ out) {
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int i = e / k, c = e - i * k;
+        out[e] = c < i ? 0.0 : (c == i ? 1.0 - 0.5 * (G[e] - 1.0) : -G[e]);
     }
 }
 
 __global__ void __launch_bounds__(kCholThreads) chol_inv_kernel(const double *__restrict__ G, int k, int n,
                                                                 int always_shift, double *__restrict__ Rinv) {
     extern __shared__ double cS[];  // k x k
+    if (!always_shift && gram_defect(G, k) < kNearIdentity) {
+        rinv_near_identity(G, k, Rinv);
+        return;
+    }
     chol_inv_block(G, k, n, always_shift, Rinv, cS);
 }
 
 __global__ void __launch_bounds__(kCholThreads) chol_inv_df_kernel(const double *__restrict__ G, int k, int n,
                                                                    int always_shift, double *__restrict__ Rinv) {
-    extern __shared__ DFp cSd[];  // k x k pairs
+    extern __shared__ DFp cSd[];  // 3 k x k pairs
+    if (!always_shift && gram_defect(G, k) < kNearIdentity) {
+        rinv_near_identity(G, k, Rinv);
+        return;
+    }
     chol_inv_df_block(G, k, n, always_shift, Rinv, cSd);
 }
 
 // The whole shifted CholeskyQR3 of the panel `a` (n x k) in one cooperative launch: per step the
 // row-block Gram partials, their sum, the k x k factor and inverse (block 0; the other blocks wait
-// at the grid barrier), and A <- A R^-1, with a grid-wide barrier between stages; after the third
+// at the grid barrier) or, for a Gram within kNearIdentity of I, its first-order inverse (every
+// block, no barrier), and A <- A R^-1, with a grid-wide barrier between stages; after the third
 // step the result is copied back into `a`.  The same stage bodies as the separate kernels, on the
 // same row blocks, so the result is bit-identical to them; it replaces 12 launches (and the copy)
 // per QR, whose launch gaps were most of a small panel's QR time.
@@ -738,16 +861,23 @@ __global__ void __launch_bounds__(256) qr_fused_kernel(double *__restrict__ a, d
     cg::grid_group grid = cg::this_grid();
     double *src = a, *dst = work;
     for (int step = 0; step < 3; ++step) {
-        if ((int)blockIdx.x < nparts) atb_block(src, src, n, k, rpb, part, blockIdx.x, (double *)qsm);
+        if ((int)blockIdx.x < nparts) atb_block(src, src, n, k, rpb, part, blockIdx.x, (double *)qsm, true);
         grid.sync();
         sum_parts_body(part, nparts, k * k, G);
         grid.sync();
-        if (blockIdx.x == 0) {
-            if (df) chol_inv_df_block(G, k, n, step == 0 ? 1 : 0, Rinv, (DFp *)qsm);
-            else chol_inv_block(G, k, n, step == 0 ? 1 : 0, Rinv, (double *)qsm);
+        // every block reads the same G, so all take the same branch (and the same grid barriers)
+        if (step > 0 && gram_defect(G, k) < kNearIdentity) {
+            rinv_near_identity(G, k, (double *)qsm);
+            __syncthreads();
+            apply_w_body(src, nullptr, n, k, dst, (double *)qsm, true);
+        } else {
+            if (blockIdx.x == 0) {
+                if (df) chol_inv_df_block(G, k, n, step == 0 ? 1 : 0, Rinv, (DFp *)qsm);
+                else chol_inv_block(G, k, n, step == 0 ? 1 : 0, Rinv, (double *)qsm);
+            }
+            grid.sync();
+            apply_w_body(src, Rinv, n, k, dst, (double *)qsm, true);
         }
-        grid.sync();
-        apply_w_body(src, Rinv, n, k, dst, (double *)qsm);
         grid.sync();
         double *t = src;
         src = dst;
@@ -766,8 +896,7 @@ __global__ void __launch_bounds__(256) qr_fused_kernel(double *__restrict__ a, d
 // A <- A R^-1, with the shift s = 11 (n k + k (k + 1)) u ||A||_F^2 in the first step, which keeps
 // the Cholesky factorization defined for condition numbers up to ~1/u (the reference's start
 // block has ~5e9), and then two plain steps (CholeskyQR2) that restore orthogonality to O(u).
-// The panel is read three times and written three times; no step needs a grid-wide barrier or
-// the host, so the QR is a dozen stream-ordered launches.  Q spans the same column space as the
+// The panel is read three times and written three times, and no step needs the host.  Q spans the same column space as the
 // reference's dgeqrf + dorgqr (methods.cpp:947-961); its columns may differ in sign, which the
 // Rayleigh-Ritz step (methods.cpp:972-1007) absorbs: the Ritz vectors come out with the
 // eigensolver's signs either way.
@@ -778,7 +907,9 @@ dpca_status launch_qr(Handle *h, double *a) {
     const bool df = k <= kEigDfMaxK;
     int nparts = 0, rpb = 0;
     gram_split(h, n, &nparts, &rpb);
-    const size_t smem = std::max<size_t>((size_t)2 * 32 * k * sizeof(double), (size_t)k * k * sizeof(double));
+    // the k x k factor's working set: S, R and R^-1 as pairs (double-float), or S in FP64
+    const size_t smem_f = df ? (size_t)3 * k * k * sizeof(DFp) : (size_t)k * k * sizeof(double);
+    const size_t smem = std::max<size_t>((size_t)2 * 32 * k * sizeof(double), smem_f);
     // one cooperative launch while the grid (the Gram's row blocks, at least one block per SM for
     // the apply) fits on the device at once; the separate kernels otherwise
     if (h->qr_coresident == 0) {
@@ -813,14 +944,14 @@ dpca_status launch_qr(Handle *h, double *a) {
         {
             ScopedLaunch t(&h->clock, h->stream, "qr_chol");
             if (df)
-                chol_inv_df_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
+                chol_inv_df_kernel<<<1, kCholThreads, smem_f, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
             else
                 chol_inv_kernel<<<1, kCholThreads, smem_g, h->stream>>>(G, k, n, step == 0 ? 1 : 0, Rinv);
             DPCA_CUDA(cudaGetLastError());
         }
         {
             ScopedLaunch t(&h->clock, h->stream, "qr_apply");
-            apply_w_kernel<<<agrid, 256, smem_g, h->stream>>>(src, Rinv, n, k, dst);
+            apply_w_kernel<<<agrid, 256, smem_g, h->stream>>>(src, Rinv, n, k, dst, 1);
             DPCA_CUDA(cudaGetLastError());
         }
         std::swap(src, dst);

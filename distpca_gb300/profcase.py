@@ -5,6 +5,8 @@
                                                 statistics and the transpose at upload, two passes
                                                 (X Omega, X^T Y), then a two-iteration solve
                                                 (Cholesky QR, Jacobi eigensolver, criterion)
+    python -m distpca_gb300.profcase small      1,000 x 100,000, nrhs 20, mixed: two passes and a
+                                                two-iteration solve (X Omega's short-K shape)
     python -m distpca_gb300.profcase windows    256 windows over 2,000 individuals, nrhs 8: the
                                                 batched windows' passes, QR and Rayleigh-Ritz kernels
     python -m distpca_gb300.profcase breakdown  per-kernel device time (the handle's kernel clock)
@@ -43,6 +45,22 @@ def incore() -> None:
         h.synchronize()
         r = h.solve(om, nsv=20, power=2, crit=1, tol=-1, miter=2, bsize=10000)
     print("incore ok, iterations", r["its"])
+
+
+def small() -> None:
+    """1,000 individuals x 100,000 SNPs, nrhs 20, mixed: two passes and a two-iteration solve (the
+    short-K shape of X Omega: 16 K-blocks per row tile)."""
+    n_ind, n_snp, k = 1000, 100000, 20
+    c = synth.make_cohort(n_ind, n_snp, n_pop=5, fst=0.05, missing=0.01, seed=0)
+    with D.Handle(n_ind, n_snp, k, precision="mixed") as h:
+        h.synth_fill(c)
+        om = D.start_block(n_ind, k)
+        h.set_omega(om)
+        h.pass_()
+        h.pass_()
+        h.synchronize()
+        r = h.solve(om, nsv=10, power=4, crit=1, tol=-1, miter=2, bsize=n_snp)
+    print("small ok, iterations", r["its"])
 
 
 def windows() -> None:
@@ -139,7 +157,7 @@ def stream() -> None:
                           "kernel_ms": {n: round(float(fam[q, f]), 1) for f, n in enumerate(names)}}), flush=True)
 
 
-CASES = {"incore": incore, "windows": windows, "breakdown": breakdown, "stream": stream}
+CASES = {"incore": incore, "small": small, "windows": windows, "breakdown": breakdown, "stream": stream}
 
 
 def main(argv=None) -> int:

@@ -138,6 +138,12 @@ dpca_status dpca_sym_eig(int k, const double *b, double *w, double *W);
  * parallel cyclic Jacobi in FP64, k <= 128), on `device`; b, w, W are host arrays as above.
  * DPCA_ERR_NUMERIC when it does not converge. */
 dpca_status dpca_sym_eig_device(int device, int k, const double *b, double *w, double *W);
+/* The thin QR every solve runs on its n x k panels (dgeqrf + dorgqr in the reference,
+ * src/methods.cpp:947-961; here shifted CholeskyQR3 on the device), on `device`: a is an n x k
+ * row-major host array, n >= 1, 1 <= k <= the nrhs limit, overwritten by Q.  separate = 1 runs
+ * the step as separate kernels instead of the one cooperative launch the solve takes when it
+ * fits; both give the same bits. */
+dpca_status dpca_qr_device(int device, int n, int k, double *a, int separate);
 
 /* ---- whole runs (device) ---- */
 /* Read <bfile>.bed/.bim/.fam and run.  omega_inout: start block in, final Ritz block out. */
