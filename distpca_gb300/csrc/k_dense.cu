@@ -14,6 +14,8 @@
 // iteration (the criterion), so the host enqueues a whole iteration ahead of the device.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include <cooperative_groups.h>
 
@@ -919,7 +921,8 @@ dpca_status launch_qr(Handle *h, double *a) {
         h->qr_coresident = std::max(1, per_sm) * h->sm_count;
         int coop = 0;
         DPCA_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
-        if (!coop || per_sm < 1) h->qr_coresident = -1;
+        const char *mode = getenv("DPCA_QR_KERNELS");
+        if (!coop || per_sm < 1 || (mode && strcmp(mode, "separate") == 0)) h->qr_coresident = -1;
     }
     const int grid = std::max(nparts, h->sm_count);
     if (h->qr_coresident > 0 && grid <= h->qr_coresident) {

@@ -358,23 +358,36 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[v], cglob & 1, err, 41, true, args.wait_cycles));
                 if (!ok) break;
                 tc::fence_after_sync();
-                // copy the accumulator out (h slices, then l slices), then release it at once
+                // copy the accumulator out (h slices, then l slices) kCols columns at a time, and
+                // release it after the last group's copy.  X Omega takes 24 columns at a time: with
+                // all kp in registers at once (2 x 48 at k = 48) the kernel reached its
+                // 128-register cap (four warps per SM sub-partition) and spilled to local memory,
+                // and its short-K tiles, whose epilogue is their cost, ran 14-21% slower.  X^T Y
+                // takes them all at once: its tiles are long, and holding the accumulator through a
+                // second copy delayed the next chunk's MMAs more than the spill cost (186 against
+                // 178 us per launch at 4,765 x 134,387, k = 40).
+                constexpr int kCols = MODE == kXW ? kDrainCols : kMaxMixedNrhs;
                 const uint32_t cb = lane_base + (uint32_t)(v * N);
-                uint32_t hv[kMaxMixedNrhs], lv[kMaxMixedNrhs];
-#pragma unroll
-                for (int j = 0; j < kMaxMixedNrhs / 8; ++j)
-                    if (8 * j < kp) {
-                        tc::tmem_ld_x8(cb + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(hv + 8 * j));
-                        tc::tmem_ld_x8(cb + kp + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(lv + 8 * j));
-                    }
-                tc::tmem_wait_ld();
-                tc::fence_before_sync();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&acc_empty[v]);
                 long long *dst = acc + (MODE == kXW ? v * kp * 128 : 0) + r;
+#pragma unroll 1
+                for (int g = 0; g < kp; g += kCols) {
+                    uint32_t hv[kCols], lv[kCols];
 #pragma unroll
-                for (int j = 0; j < kMaxMixedNrhs; ++j)
-                    if (j < kp) dst[j * 128] += slices_int(hv[j], lv[j]);
+                    for (int j = 0; j < kCols / 8; ++j)
+                        if (g + 8 * j < kp) {
+                            tc::tmem_ld_x8(cb + g + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(hv + 8 * j));
+                            tc::tmem_ld_x8(cb + kp + g + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(lv + 8 * j));
+                        }
+                    tc::tmem_wait_ld();
+                    if (g + kCols >= kp) {
+                        tc::fence_before_sync();
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&acc_empty[v]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < kCols; ++j)
+                        if (g + j < kp) dst[(g + j) * 128] += slices_int(hv[j], lv[j]);
+                }
             }
             const bool valid = ok && row < args.rows;
             const double *sc = args.scales + (size_t)x.win * 4 * k;

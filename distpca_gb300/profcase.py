@@ -13,6 +13,8 @@
                                                 of whole converged solves: the 1,000 x 100,000
                                                 cohort (nsv 10, nrhs 20, power 4, tol 1e-6) and
                                                 two serving-size jobs, mixed and FP64
+    python -m distpca_gb300.profcase passes     per-launch device time of a mixed pass's kernels at
+                                                four serving-size shapes
     python -m distpca_gb300.profcase stream     the 512 jobs of the serving stream (serve_stream,
                                                 seed 0) solved one at a time, mixed: wall time,
                                                 then per-kernel device time summed over the jobs
@@ -100,6 +102,30 @@ def breakdown() -> None:
                               "kernel_ms_total": round(tot, 2), "per_kernel_ms_launches": per}), flush=True)
 
 
+PASS_SHAPES = [(1000, 100000, 20), (2813, 37351, 10), (4765, 134387, 40), (20000, 100000, 40)]
+
+
+def passes() -> None:
+    """Per-launch device time of a mixed pass's kernels at serving-size shapes: 3 warm-up passes,
+    then 20 under the per-launch clock."""
+    out = {}
+    for n, m, k in PASS_SHAPES:
+        c = synth.make_cohort(n, m, n_pop=4, fst=0.05, missing=0.01, seed=1)
+        with D.Handle(n, m, k, precision="mixed") as h:
+            h.synth_fill(c)
+            h.set_omega(D.start_block(n, k))
+            for _ in range(3):
+                h.pass_()
+            h.synchronize()
+            h.reset_kernel_times(True)
+            for _ in range(20):
+                h.pass_()
+            h.synchronize()
+            kt = h.kernel_times()
+        out[f"{n}x{m}_nrhs{k}"] = {a: round(v["ms"] / v["launches"] * 1e3, 1) for a, v in kt.items() if v["launches"]}
+    print(json.dumps({"us_per_launch": out}))
+
+
 def _kernel_family(name: str) -> str:
     if name in ("mixed_xw", "mixed_xty", "mixed_reduce", "split_omega", "split_bop"):
         return "products"
@@ -157,7 +183,8 @@ def stream() -> None:
                           "kernel_ms": {n: round(float(fam[q, f]), 1) for f, n in enumerate(names)}}), flush=True)
 
 
-CASES = {"incore": incore, "small": small, "windows": windows, "breakdown": breakdown, "stream": stream}
+CASES = {"incore": incore, "small": small, "windows": windows, "breakdown": breakdown, "stream": stream,
+         "passes": passes}
 
 
 def main(argv=None) -> int:
