@@ -39,9 +39,8 @@ constexpr int kSmemBudget = 220 * 1024;
 constexpr int kChunkG = 32;              // f2 (= g') accumulator
 constexpr int kChunkM = 32;              // f1 accumulator
 constexpr int kFirstChunkM = 16;         // staggers the f1 drains against the f2 drains
-constexpr int kMaxMixedNrhs = 48;
-constexpr int kDrainCols = 24;  // accumulator columns the drain copies to registers at a time (x8 loads)
-constexpr int kEpiCols = 4;     // X Omega epilogue columns per step of its loop        // accumulators 2 x N <= 192 columns + 2 A stages of 128
+constexpr int kMaxMixedNrhs = 48;        // accumulators 2 x N <= 192 columns + 2 A stages of 128
+constexpr int kDrainCols = 24;           // accumulator columns the X Omega drain copies at a time
 
 struct GemmArgs {
     int rows;          // valid output rows
