@@ -13,6 +13,8 @@
                                                 of whole converged solves: the 1,000 x 100,000
                                                 cohort (nsv 10, nrhs 20, power 4, tol 1e-6) and
                                                 two serving-size jobs, mixed and FP64
+    python -m distpca_gb300.profcase qr         the device QR of random panels at four shapes, as one
+                                                launch and as separate kernels (for a launch list)
     python -m distpca_gb300.profcase passes     per-launch device time of a mixed pass's kernels at
                                                 four serving-size shapes
     python -m distpca_gb300.profcase stream     the 512 jobs of the serving stream (serve_stream,
@@ -103,6 +105,19 @@ def breakdown() -> None:
 
 
 PASS_SHAPES = [(1000, 100000, 20), (2813, 37351, 10), (4765, 134387, 40), (20000, 100000, 40)]
+QR_SHAPES = [(1000, 10), (1000, 20), (4765, 40), (20000, 40)]
+
+
+def qr() -> None:
+    """The device QR of random panels at serving-size shapes, twice as one cooperative launch and
+    twice as separate kernels (for a per-kernel launch list); prints max |Q^T Q - I|."""
+    rng = np.random.default_rng(0)
+    for n, k in QR_SHAPES:
+        a = rng.standard_normal((n, k))
+        for separate in (False, True):
+            for _ in range(2):
+                q = D.qr_device(a, separate=separate)
+        print(n, k, float(np.abs(q.T @ q - np.eye(k)).max()))
 
 
 def passes() -> None:
@@ -184,7 +199,7 @@ def stream() -> None:
 
 
 CASES = {"incore": incore, "small": small, "windows": windows, "breakdown": breakdown, "stream": stream,
-         "passes": passes}
+         "passes": passes, "qr": qr}
 
 
 def main(argv=None) -> int:
