@@ -311,8 +311,10 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const double *__re
 // bound the FP64 kernel on its one SM together with the rotations' dependent FP64 division and
 // square-root chains (a warp's FP64 instruction occupies the narrow FP64 pipe for many cycles).
 // The rotations are formed in double-float too, from reciprocal square roots and quotients
-// refined by Newton steps in pairs (dfp_rsqrt, dfp_div_fast).  The relative skip test uses 2^-44 in place of FP64's epsilon, with an absolute
-// floor of 2^-47, so the sweeps end at the pairs' precision.  B is scaled by a power of two to
+// refined by Newton steps in pairs (dfp_rsqrt, dfp_div_fast).  A round is two barrier-separated
+// steps: the rotations, then A <- J^T A J on 2 x 2 blocks (rows, then columns) together with
+// V <- V J.  The relative skip test uses 2^-44 in place of FP64's epsilon, with an absolute floor
+// of 2^-47, so the sweeps end at the pairs' precision.  B is scaled by a power of two to
 // max |b| in [1/2, 1) first (FP32's exponent range), and the eigenvalues scaled back exactly.
 // Each rotation's c^2 + s^2 is 1 within ~2^-45, and that error compounds over the ~2k rotations an
 // entry takes per sweep: eigenvalues and eigenvectors come out within 1e-12 of max |w| up to k = 48
@@ -482,30 +484,54 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_df_kernel(const double *_
                 sn[tid] = s;
             }
             __syncthreads();
-            // rows p, q of A (the element walk of sym_eig_kernel)
-            for (int i = i0, j = j0; i < npairs;) {
-                const DFp s = sn[i];
-                if (s.hi != 0.f) {
-                    const DFp c = cs[i], ms = DFp{-s.hi, -s.lo};
-                    const int p = pp[i], q = qq[i];
-                    const DFp ap = A[p * k + j], aq = A[q * k + j];
-                    A[p * k + j] = dfp_dot2(c, ap, ms, aq);
-                    A[q * k + j] = dfp_dot2(s, ap, c, aq);
+            // A <- J^T A J on the 2 x 2 blocks (pair P rows, pair Q columns), one block per thread:
+            // the rows by P's rotation, then the columns by Q's, as separate row and column passes
+            // would do them (the same operations, so the same bits), with one barrier instead of
+            // two; the annihilated pair is set to zero exactly.  V <- V J in the same step.
+            for (int bq = tid; bq < npairs * npairs; bq += kEigThreads) {
+                const int P = bq / npairs, Q = bq - P * npairs;
+                const DFp sP = sn[P], sQ = sn[Q];
+                if (sP.hi == 0.f && sQ.hi == 0.f) continue;
+                const int x0 = pp[P], x1 = qq[P], y0 = pp[Q], y1 = qq[Q];  // x1, y1 may be the pad k
+                const bool vx1 = x1 < k, vy1 = y1 < k;
+                DFp e00 = A[x0 * k + y0], e01 = vy1 ? A[x0 * k + y1] : DFp{0.f, 0.f};
+                DFp e10 = vx1 ? A[x1 * k + y0] : DFp{0.f, 0.f};
+                DFp e11 = vx1 && vy1 ? A[x1 * k + y1] : DFp{0.f, 0.f};
+                if (sP.hi != 0.f) {  // rows x0, x1 (both real when P rotates)
+                    const DFp c = cs[P], ms = DFp{-sP.hi, -sP.lo};
+                    DFp t0 = dfp_dot2(c, e00, ms, e10), t1 = dfp_dot2(sP, e00, c, e10);
+                    e00 = t0;
+                    e10 = t1;
+                    if (vy1) {
+                        t0 = dfp_dot2(c, e01, ms, e11);
+                        t1 = dfp_dot2(sP, e01, c, e11);
+                        e01 = t0;
+                        e11 = t1;
+                    }
                 }
-                i += di;
-                j += dj;
-                if (j >= k) j -= k, ++i;
+                if (sQ.hi != 0.f) {  // columns y0, y1 (both real when Q rotates)
+                    const DFp c = cs[Q], ms = DFp{-sQ.hi, -sQ.lo};
+                    DFp t0 = x0 == y1 ? DFp{0.f, 0.f} : dfp_dot2(c, e00, ms, e01);
+                    DFp t1 = x0 == y0 ? DFp{0.f, 0.f} : dfp_dot2(sQ, e00, c, e01);
+                    e00 = t0;
+                    e01 = t1;
+                    if (vx1) {
+                        t0 = x1 == y1 ? DFp{0.f, 0.f} : dfp_dot2(c, e10, ms, e11);
+                        t1 = x1 == y0 ? DFp{0.f, 0.f} : dfp_dot2(sQ, e10, c, e11);
+                        e10 = t0;
+                        e11 = t1;
+                    }
+                }
+                A[x0 * k + y0] = e00;
+                if (vy1) A[x0 * k + y1] = e01;
+                if (vx1) A[x1 * k + y0] = e10;
+                if (vx1 && vy1) A[x1 * k + y1] = e11;
             }
-            __syncthreads();
-            // columns p, q of A and V; the annihilated pair is set to zero exactly
             for (int i = i0, j = j0; i < npairs;) {
                 const DFp s = sn[i];
                 if (s.hi != 0.f) {
                     const DFp c = cs[i], ms = DFp{-s.hi, -s.lo};
                     const int p = pp[i], q = qq[i];
-                    const DFp ap = A[j * k + p], aq = A[j * k + q];
-                    A[j * k + p] = j == q ? DFp{0.f, 0.f} : dfp_dot2(c, ap, ms, aq);
-                    A[j * k + q] = j == p ? DFp{0.f, 0.f} : dfp_dot2(s, ap, c, aq);
                     const DFp vp = V[j * k + p], vq = V[j * k + q];
                     V[j * k + p] = dfp_dot2(c, vp, ms, vq);
                     V[j * k + q] = dfp_dot2(s, vp, c, vq);
