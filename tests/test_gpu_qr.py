@@ -53,6 +53,26 @@ def test_qr_ill_conditioned(dpca, n, k):
     assert np.array_equal(q, dpca.qr_device(a, separate=True))
 
 
+def test_qr_rank_deficient_panel(dpca):
+    """A column that is an exact combination of earlier ones (a full-width block of a cohort with
+    fewer directions than columns): the independent columns still come out orthonormal and exact,
+    and the dependent one finite and orthogonal to them."""
+    rng = np.random.default_rng(11)
+    n, k = 2000, 24
+    a = rng.standard_normal((n, k))
+    a[:, 13] = a[:, 2] - 0.5 * a[:, 7]  # column 13 depends on columns 2 and 7
+    q = dpca.qr_device(a)
+    assert np.all(np.isfinite(q))
+    good = [c for c in range(k) if c != 13]
+    qg = q[:, good]
+    assert np.abs(qg.T @ qg - np.eye(k - 1)).max() < 5e-12
+    # the first 13 columns span exactly a's first 13
+    ql, _ = np.linalg.qr(a[:, :13])
+    np.testing.assert_allclose(np.abs(ql.T @ q[:, :13]), np.eye(13), atol=1e-9)
+    assert np.abs(qg.T @ q[:, 13]).max() < 1e-6 * max(1.0, np.linalg.norm(q[:, 13]))
+    assert np.array_equal(q, dpca.qr_device(a, separate=True))
+
+
 def test_qr_scale_invariant(dpca):
     """The k x k factor runs on the Gram scaled by a power of two: panels of 1e-150 and 1e150 give
     Q as for the unit panel."""
