@@ -207,6 +207,7 @@ struct Handle {
     // Coarse timing of a solve's stages (a pass's two products, a QR, the eigensolve) when the
     // per-launch clock is off: a few events per outer iteration instead of two per launch.
     KernelClock *stage = nullptr;
+    bool no_graphs = false;  // solves launch every iteration eagerly (serving handles)
     int qr_coresident = 0;  // blocks of the fused QR kernel that fit at once (0: not queried, -1: none)
 };
 

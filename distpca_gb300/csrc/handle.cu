@@ -8,6 +8,7 @@
 // device; the host reads back nsv singular values and the criterion flag once per iteration.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <set>
@@ -350,6 +351,7 @@ dpca_status create_serving_handle(dpca_handle **out, int n_ind, int n_snp, int n
     // jobs' kernels off those SMs.  On the 512-job serving stream: 37.4 jobs/s with the one-launch
     // QR, 43.8 with the separate kernels.
     hh->h.qr_coresident = -1;
+    hh->h.no_graphs = true;
     dpca_status st = create_impl(&hh->h, n_ind, n_snp, nrhs, precision, device, stream, 0);
     if (st != DPCA_OK) {
         free_all(&hh->h);
@@ -529,6 +531,9 @@ static double slot_ms(const KernelClock &c, const char *name) {
     return 0.0;
 }
 
+// Outer iterations launched eagerly before a solve replays them as graphs.
+constexpr int kGraphFromIter = 3;
+
 static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_inout, dpca_result *res) {
     const int n = h->n_ind, k = h->k;
     if (!cfg || !omega_inout || !res) {
@@ -588,7 +593,10 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     double *omega = h->omega, *z = h->z, *q = h->q;
     int ii = 0, passes = 0;
     bool stopped = false;
-    for (ii = 0; ii < miter; ++ii) {
+    // The device work of one outer iteration: the passes and QRs, the Rayleigh-Ritz step and the
+    // criterion.  `iter` matters only as iter > 0 (the criterion compares with the iteration
+    // before).  Rotates omega, z, q and counts the passes as it goes.
+    auto body = [&](int iter) -> dpca_status {
         DPCA_TRY(handle_pass_io(h, omega, z));
         passes++;
         for (int kk = 0; kk < power - 1; ++kk) {
@@ -620,7 +628,78 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
             ScopedLaunch t(h->stage, h->stream, "apply_w");
             DPCA_TRY(launch_apply_w(h, q, omega));
         }
-        DPCA_TRY(launch_sigma_and_criterion(h, nsv, crit, cfg->tol, ii, h->old, omega));
+        return launch_sigma_and_criterion(h, nsv, crit, cfg->tol, iter, h->old, omega);
+    };
+    // Iteration graphs.  From the kGraphFromIter-th outer iteration on, an iteration's ~40 launches
+    // replay as one CUDA graph: the kernels are the same, in the same order, so the results are
+    // the same bits, and the gaps between dependent launches shrink.  An iteration rotates the
+    // three n x k buffers, so a graph is captured for each assignment of them that occurs (at
+    // most three) the first time it does.  Not for streamed handles (a pass reads host blocks),
+    // under the per-launch clock, while a test fault is pending, nor on serving handles, whose
+    // short solves would spend more on capture than they save.  A capture that fails leaves the
+    // solve on eager launches.
+    struct IterGraph {
+        double *pre[3], *post[3];
+        cudaGraphExec_t exec;
+        int passes;
+    };
+    std::vector<IterGraph> graphs;
+    struct GraphsGuard {
+        std::vector<IterGraph> &g;
+        ~GraphsGuard() {
+            for (auto &x : g) cudaGraphExecDestroy(x.exec);
+        }
+    } graphs_guard{graphs};
+    const char *genv = getenv("DPCA_SOLVE_GRAPHS");
+    bool use_graphs = !fine && !h->streamed && !h->no_graphs && h->inject_fault == 0 && miter > kGraphFromIter &&
+                      !(genv && strcmp(genv, "0") == 0);
+    auto capture = [&]() -> const IterGraph * {
+        double *pre[3] = {omega, z, q};
+        const int passes0 = passes;
+        if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        KernelClock *stage = h->stage;
+        h->stage = nullptr;
+        const dpca_status st = body(1);
+        h->stage = stage;
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        cudaGraphExec_t exec = nullptr;
+        if (st == DPCA_OK && e == cudaSuccess && g && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
+        if (g) cudaGraphDestroy(g);
+        IterGraph entry{{pre[0], pre[1], pre[2]}, {omega, z, q}, exec, passes - passes0};
+        omega = pre[0];  // the captured work has not run
+        z = pre[1];
+        q = pre[2];
+        passes = passes0;
+        if (!exec) {
+            cudaGetLastError();
+            clear_error();
+            return nullptr;
+        }
+        graphs.push_back(entry);
+        return &graphs.back();
+    };
+    for (ii = 0; ii < miter; ++ii) {
+        const IterGraph *gi = nullptr;
+        if (use_graphs && ii >= kGraphFromIter) {
+            for (const auto &x : graphs)
+                if (x.pre[0] == omega && x.pre[1] == z && x.pre[2] == q) gi = &x;
+            if (!gi) gi = capture();
+            if (!gi) use_graphs = false;
+        }
+        if (gi) {
+            ScopedLaunch t(h->stage, h->stream, "graph_iterations");
+            DPCA_CUDA(cudaGraphLaunch(gi->exec, h->stream));
+            omega = gi->post[0];
+            z = gi->post[1];
+            q = gi->post[2];
+            passes += gi->passes;
+        } else {
+            DPCA_TRY(body(ii));
+        }
         DPCA_CUDA(cudaMemcpyAsync(h->host_small, h->small, L.total() * sizeof(double), cudaMemcpyDeviceToHost,
                                   h->stream));
         DPCA_CUDA(cudaStreamSynchronize(h->stream));
@@ -674,6 +753,18 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     res->time_gs = (slot_ms(c, "qr_gram") + slot_ms(c, "qr_gram_sum") + slot_ms(c, "qr_chol") +
                     slot_ms(c, "qr_apply") + slot_ms(c, "qr_fused")) * 1e-3;
     res->time_projected_svd = slot_ms(c, "sym_eig") * 1e-3;
+    // graph-replayed iterations are timed as a whole: their time is split among the stages in the
+    // proportions of the eagerly launched iterations
+    const double staged = res->time_mm + res->time_gs + res->time_projected_svd;
+    const double graphed = slot_ms(c, "graph_iterations") * 1e-3;
+    if (graphed > 0.0 && staged > 0.0) {
+        const double f = (staged + graphed) / staged;
+        res->time_mm_a *= f;
+        res->time_mm_a_t *= f;
+        res->time_mm *= f;
+        res->time_gs *= f;
+        res->time_projected_svd *= f;
+    }
     res->time_other = total_ms * 1e-3 - res->time_mm - res->time_gs - res->time_projected_svd;
     if (res->time_other < 0) res->time_other = 0;
     h->clock.enabled = clock_was;

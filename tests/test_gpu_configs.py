@@ -143,6 +143,22 @@ def test_cfg1_mixed_converged_pca(dpca, configs, cfg1_packed, run):
     check_mixed(r, configs, run, CFG1_LEAD, its_slack=max(1, int(0.1 * int(configs[f"run_{run}_its"]))))
 
 
+@pytest.mark.parametrize("run,precision", [("cfg1", "mixed"), ("cfg1_mev", "mixed"), ("cfg1_fixed4", "fp64")])
+def test_cfg1_iteration_graphs_same_bits(dpca, configs, cfg1_packed, monkeypatch, run, precision):
+    """From the fourth outer iteration on, a solve replays each iteration as a CUDA graph of the
+    same launches: sigma, U and the iteration count must be those of eager launches, bit for bit
+    (crit 2 also copies the Ritz block between the replays)."""
+    fl = flags_of(configs, run)
+    kw = solve_kw(fl, precision)
+    monkeypatch.setenv("DPCA_SOLVE_GRAPHS", "0")
+    eager = dpca.run_packed(cfg1_packed, CFG1["n_ind"], **kw)
+    monkeypatch.delenv("DPCA_SOLVE_GRAPHS")
+    graphed = dpca.run_packed(cfg1_packed, CFG1["n_ind"], **kw)
+    assert graphed["its"] == eager["its"] and graphed["its"] >= 4
+    assert np.array_equal(graphed["sigma"], eager["sigma"])
+    assert np.array_equal(graphed["u"], eager["u"])
+
+
 # HGDP: the published log's 22 passes are 11 outer iterations of power + 1 = 2 passes
 HGDP_LEAD = 5
 
