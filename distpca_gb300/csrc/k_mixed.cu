@@ -72,7 +72,9 @@ static dpca_status launch_xw(Handle *h, const CUtensorMap &map_a, const CUtensor
 // issuers' "stage free" commits are multicast to every CTA (free_ counts 2 CL commits).  The
 // CTAs meet at a cluster barrier after barrier initialisation (no remote arrival may reach an
 // uninitialised barrier) and before exit (no multicast may land in an exited CTA's memory).
-template <int MODE, int CL>
+// DC: the accumulator columns the drain copies to registers at a time (kDrainCols or
+// kMaxMixedNrhs; see the drain).
+template <int MODE, int CL, int DC = (MODE == kXW ? kDrainCols : kMaxMixedNrhs)>
 __global__ void __launch_bounds__(kThreads, 1)
     mixed_gemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                       const GemmArgs args) {
@@ -358,15 +360,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[v], cglob & 1, err, 41, true, args.wait_cycles));
                 if (!ok) break;
                 tc::fence_after_sync();
-                // copy the accumulator out (h slices, then l slices) kCols columns at a time, and
-                // release it after the last group's copy.  X Omega takes 24 columns at a time: with
-                // all kp in registers at once (2 x 48 at k = 48) the kernel reached its
-                // 128-register cap (four warps per SM sub-partition) and spilled to local memory,
-                // and its short-K tiles, whose epilogue is their cost, ran 14-21% slower.  X^T Y
-                // takes them all at once: its tiles are long, and holding the accumulator through a
-                // second copy delayed the next chunk's MMAs more than the spill cost (186 against
-                // 178 us per launch at 4,765 x 134,387, k = 40).
-                constexpr int kCols = MODE == kXW ? kDrainCols : kMaxMixedNrhs;
+                // copy the accumulator out (h slices, then l slices) DC columns at a time, and
+                // release it after the last group's copy.  X Omega over up to kLongKIndividuals
+                // takes 24 columns at a time: with all kp in registers at once (2 x 48 at k = 48)
+                // the kernel reached its 128-register cap (four warps per SM sub-partition) and
+                // spilled to local memory, and its short-K tiles, whose epilogue is their cost, ran
+                // 14-21% slower.  Long tiles (X^T Y; X Omega over more individuals) take them all at
+                // once: holding the accumulator through a second copy delays the next chunk's MMAs
+                // more than the spill costs (X^T Y: 186 against 178 us per launch at 4,765 x
+                // 134,387, k = 40; X Omega at 50,000 x 1,000,000: 11.36 against 11.13 ms).
+                constexpr int kCols = DC;
                 const uint32_t cb = lane_base + (uint32_t)(v * N);
                 long long *dst = acc + (MODE == kXW ? v * kp * 128 : 0) + r;
 #pragma unroll 1
@@ -854,6 +857,8 @@ dpca_status mixed_prepare(Handle *h) {
     DPCA_TRY(make_batch_map(&m->map_bop_band[1], m->bop, rows_pad, 2 * N, (uint32_t)(N / 2), 1));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW, 1>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW, 2>));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW, 1, kMaxMixedNrhs>));
+    DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXW, 2, kMaxMixedNrhs>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 1>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 2>));
     DPCA_TRY(allow_max_smem((const void *)mixed_gemm_kernel<kXTY, 4>));
@@ -969,10 +974,15 @@ static dpca_status launch_xw(Handle *h, const CUtensorMap &map_a, const CUtensor
         if (v == 1 || v == 2) cl = v;
     }
     const int tiles = ceil_div(a.rows, 128);
+    const bool long_k = h->n_ind >= kLongKIndividuals;
     if (cl == 0) cl = 1;
     if (cl == 1 || tiles < 2) {
         a.tiles = a.items = tiles;
-        mixed_gemm_kernel<kXW, 1><<<std::min(a.items, h->sm_count), kThreads, m->smem1, h->stream>>>(map_a, map_b, a);
+        const int grid = std::min(a.items, h->sm_count);
+        if (long_k)
+            mixed_gemm_kernel<kXW, 1, kMaxMixedNrhs><<<grid, kThreads, m->smem1, h->stream>>>(map_a, map_b, a);
+        else
+            mixed_gemm_kernel<kXW, 1><<<grid, kThreads, m->smem1, h->stream>>>(map_a, map_b, a);
         DPCA_CUDA(cudaGetLastError());
         return DPCA_OK;
     }
@@ -997,7 +1007,10 @@ static dpca_status launch_xw(Handle *h, const CUtensorMap &map_a, const CUtensor
         }
     }
     cfg.gridDim = dim3(std::min(a.items, 2 * m->xw_max_clusters));
-    DPCA_CUDA(cudaLaunchKernelEx(&cfg, mixed_gemm_kernel<kXW, 2>, map_a, map_b_band, a));
+    if (long_k)
+        DPCA_CUDA(cudaLaunchKernelEx(&cfg, mixed_gemm_kernel<kXW, 2, kMaxMixedNrhs>, map_a, map_b_band, a));
+    else
+        DPCA_CUDA(cudaLaunchKernelEx(&cfg, mixed_gemm_kernel<kXW, 2>, map_a, map_b_band, a));
     return DPCA_OK;
 }
 

@@ -41,6 +41,7 @@ constexpr int kChunkM = 32;              // f1 accumulator
 constexpr int kFirstChunkM = 16;         // staggers the f1 drains against the f2 drains
 constexpr int kMaxMixedNrhs = 48;        // accumulators 2 x N <= 192 columns + 2 A stages of 128
 constexpr int kDrainCols = 24;           // accumulator columns the X Omega drain copies at a time
+constexpr int kLongKIndividuals = 32768; // X Omega over at least this many individuals drains at once
 
 struct GemmArgs {
     int rows;          // valid output rows

@@ -42,8 +42,11 @@ def test_pass_matches_oracle(dpca, oracle, name, k):
 
 
 @pytest.mark.parametrize("n_ind,n_snp,k", [(5, 7, 2), (129, 513, 3), (517, 2049, 17), (1000, 3001, 40),
-                                           (2048, 4099, 48), (3001, 1500, 33), (64, 20000, 8)])
+                                           (2048, 4099, 48), (3001, 1500, 33), (64, 20000, 8),
+                                           (33001, 700, 48), (40000, 1031, 20)])
 def test_pass_ragged_shapes_vs_fp64(dpca, n_ind, n_snp, k):
+    """Ragged shapes; 33,001 and 40,000 individuals take X Omega's long-K variant (the accumulator
+    drained in one copy)."""
     from distpca_gb300 import synth
 
     c = synth.make_cohort(n_ind, n_snp, n_pop=3, fst=0.05, missing=0.03, seed=n_ind + n_snp)
