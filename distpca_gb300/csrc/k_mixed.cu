@@ -372,6 +372,22 @@ __global__ void __launch_bounds__(kThreads, 1)
                 constexpr int kCols = DC;
                 const uint32_t cb = lane_base + (uint32_t)(v * N);
                 long long *dst = acc + (MODE == kXW ? v * kp * 128 : 0) + r;
+                if constexpr (kCols >= kMaxMixedNrhs) {  // one copy
+                    uint32_t hv[kMaxMixedNrhs], lv[kMaxMixedNrhs];
+#pragma unroll
+                    for (int j = 0; j < kMaxMixedNrhs / 8; ++j)
+                        if (8 * j < kp) {
+                            tc::tmem_ld_x8(cb + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(hv + 8 * j));
+                            tc::tmem_ld_x8(cb + kp + 8 * j, *reinterpret_cast<uint32_t(*)[8]>(lv + 8 * j));
+                        }
+                    tc::tmem_wait_ld();
+                    tc::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&acc_empty[v]);
+#pragma unroll
+                    for (int j = 0; j < kMaxMixedNrhs; ++j)
+                        if (j < kp) dst[j * 128] += slices_int(hv[j], lv[j]);
+                } else
 #pragma unroll 1
                 for (int g = 0; g < kp; g += kCols) {
                     uint32_t hv[kCols], lv[kCols];
