@@ -56,13 +56,15 @@ struct KernelClock {
     ~KernelClock();
 };
 
-// Scoped timing of one launch: records events around the enclosed launch when enabled.
+// Scoped timing of one launch: records events around the enclosed launch when enabled, and counts
+// `kernels` launches for it (the kernels the scope encloses).
 struct ScopedLaunch {
     KernelClock *clk;
     cudaStream_t st;
     int slot = -1;
+    int kernels = 1;
     cudaEvent_t a = nullptr, b = nullptr;
-    ScopedLaunch(KernelClock *c, cudaStream_t s, const char *name);
+    ScopedLaunch(KernelClock *c, cudaStream_t s, const char *name, int kernels = 1);
     ~ScopedLaunch();
 };
 

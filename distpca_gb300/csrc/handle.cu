@@ -64,7 +64,7 @@ KernelClock::~KernelClock() {
     for (auto e : pool) cudaEventDestroy(e);
 }
 
-ScopedLaunch::ScopedLaunch(KernelClock *c, cudaStream_t s, const char *name) : clk(c), st(s) {
+ScopedLaunch::ScopedLaunch(KernelClock *c, cudaStream_t s, const char *name, int n) : clk(c), st(s), kernels(n) {
     if (!clk || !clk->enabled) return;
     slot = clk->slot(name);
     a = clk->get_event();
@@ -75,7 +75,7 @@ ScopedLaunch::ScopedLaunch(KernelClock *c, cudaStream_t s, const char *name) : c
 ScopedLaunch::~ScopedLaunch() {
     if (slot < 0) return;
     cudaEventRecord(b, st);
-    clk->launches[slot]++;
+    clk->launches[slot] += kernels;
     clk->pending.push_back({slot, a, b});
 }
 

@@ -915,7 +915,7 @@ dpca_status mixed_release(Handle *h) {
 dpca_status mixed_omega_operand(Handle *h, const double *omega) {
     MixedState *m = mstate(h);
     const int k = h->k;
-    ScopedLaunch t(&h->clock, h->stream, "split_omega");
+    ScopedLaunch t(&h->clock, h->stream, "split_omega", 2);  // the scales and the split
     omega_scales_kernel<<<k, 256, 0, h->stream>>>(omega, h->n_ind, k, m->scales);
     int64_t total = (int64_t)m->kp * h->n_ind_pad;
     int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 8);
