@@ -635,9 +635,9 @@ static dpca_status solve_impl(Handle *h, const dpca_config *cfg, double *omega_i
     // the same bits, and the gaps between dependent launches shrink.  An iteration rotates the
     // three n x k buffers, so a graph is captured for each assignment of them that occurs (at
     // most three) the first time it does.  Not for streamed handles (a pass reads host blocks),
-    // under the per-launch clock, while a test fault is pending, nor on serving handles, whose
-    // short solves would spend more on capture than they save.  A capture that fails leaves the
-    // solve on eager launches.
+    // under the per-launch clock, while a test fault is pending, nor on serving handles (short
+    // solves, on a device whose launch gaps the other jobs' kernels fill; not measured there).  A
+    // capture that fails leaves the solve on eager launches.
     struct IterGraph {
         double *pre[3], *post[3];
         cudaGraphExec_t exec;
