@@ -268,3 +268,19 @@ def test_windows_reject_bad_shapes_before_the_device(dpca):
     with pytest.raises(dpca.DpcaError) as e:
         dpca.Windows(500, [1000], 64)
     assert e.value.status == 6
+
+
+def test_device_utilities_reject_bad_arguments_before_any_device_work(dpca):
+    """dpca_qr_device and dpca_sym_eig_device check their arguments first: bad ones return
+    DPCA_ERR_INVALID (1) with a message, with or without a GPU."""
+    lib = dpca.lib()
+    a = np.zeros((4, 2))
+    p = a.ctypes.data_as(ctypes.c_void_p)
+    assert lib.dpca_qr_device(0, 4, 0, p, 0) == 1  # k = 0
+    assert lib.dpca_qr_device(0, 0, 2, p, 0) == 1  # n = 0
+    assert lib.dpca_qr_device(0, 4, 2, None, 0) == 1  # no array
+    assert lib.dpca_qr_device(0, 4, 100000, p, 0) == 1  # k above the limit
+    assert b"dpca_qr_device" in lib.dpca_last_error()
+    w = np.zeros(2)
+    assert lib.dpca_sym_eig_device(0, 0, p, w.ctypes.data_as(ctypes.c_void_p), p) == 1
+    assert lib.dpca_sym_eig_device(0, 2, None, None, None) == 1
